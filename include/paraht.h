@@ -1,0 +1,112 @@
+/*
+ * paraht.h -- C ABI of the GB300 (sm_103a) two-stage Hessenberg-triangular reduction.
+ *
+ * Reduces a real pencil (A, B), B upper triangular, to (H, T) = (Q^T A Z, Q^T B Z) with H upper
+ * Hessenberg and T upper triangular, in two stages:
+ *   stage 1  (A, B) -> (r-Hessenberg, triangular)    replaces ab2rht_simple, src/ab2rht.f90:8
+ *   stage 2  r-Hessenberg -> Hessenberg              replaces rht2ht_householder, src/rht2ht.f90:1346
+ * Q and Z are ACCUMULATED: both stages right-multiply the Q and Z they receive (pass identity
+ * matrices for the plain transforms), exactly as the reference does.
+ *
+ * Layout: column-major FP64 with leading dimensions, like the reference's Fortran arrays
+ * A(lda,*).  All integers are plain C ints passed by value (a Fortran caller uses bind(C) with
+ * the VALUE attribute; see the Fortran module shipped with the library).
+ *
+ * Errors: every entry point returns an int status, 0 on success.  A negative value -i in
+ * [-20,-1] names the invalid i-th argument, as LAPACK's INFO does; values <= -1000 are the
+ * PARAHT_ERR_* codes below.  The reference has no error reporting (LAPACK INFO is ignored,
+ * src/ab2rht.f90:105, :291); nothing here aborts the process.
+ *
+ * Valid parameters (checked): n >= 1; 1 <= r <= 64; p >= 2; 1 <= nq <= r.  Stage 2 must be
+ * given the same r that stage 1 used (src/profilereduction.f90:136, :144).  nq > r lies
+ * outside the domain where the reference's staircase bookkeeping (src/rht2ht.f90:1649-1675,
+ * :1823-1829) stays consistent: its results lose accuracy for some n, so it is rejected.
+ *
+ * Threading: entry points taking a paraht_ctx are thread-safe per context (one stream per
+ * context, no global state).  The context-free host entry points use one lazily created
+ * context per calling host thread on the current CUDA device.
+ */
+#ifndef PARAHT_H
+#define PARAHT_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PARAHT_VERSION 100 /* 1.0.0 */
+
+/* ---- status codes ---- */
+#define PARAHT_OK 0
+#define PARAHT_ERR_CUDA (-1001)          /* a CUDA runtime call failed */
+#define PARAHT_ERR_ALLOC (-1002)         /* device or pinned-host allocation failed */
+#define PARAHT_ERR_TIMEOUT (-1003)       /* a bounded device-side wait expired */
+#define PARAHT_ERR_NONFINITE (-1004)     /* NaN/Inf found in the input (PARAHT_FLAG_CHECK_FINITE) */
+#define PARAHT_ERR_NOT_SUPPORTED (-1005) /* parameter combination not supported on this device */
+#define PARAHT_ERR_NO_DEVICE (-1006)     /* no usable CUDA device */
+#define PARAHT_ERR_BAD_CTX (-1007)       /* null or destroyed context */
+
+/* ---- flags (bit set) ---- */
+#define PARAHT_FLAG_TIME_COMPONENTS 1 /* record per-phase times (time_components, src/ab2rht.f90:13) */
+#define PARAHT_FLAG_CHECK_FINITE 2    /* reject non-finite inputs before reducing */
+#define PARAHT_FLAG_SPLIT 4           /* split-precision (emulated FP64) bulk updates */
+#define PARAHT_FLAG_NO_ZERO_FILL 8    /* keep roundoff below the structure instead of exact zeros */
+
+typedef struct paraht_ctx_s* paraht_ctx;
+
+/* ---- context ---- */
+int paraht_ctx_create(paraht_ctx* ctx, int device);
+int paraht_ctx_destroy(paraht_ctx ctx);
+/* Use an existing cudaStream_t (passed as void*); NULL selects the context's own stream. */
+int paraht_ctx_set_stream(paraht_ctx ctx, void* stream);
+/* Phase times of the last call, in seconds, when PARAHT_FLAG_TIME_COMPONENTS was set:
+ *   [0] stage-1 left generation  [1] stage-1 right generation  [2] stage-1 multiplications
+ *   [3] stage-2 generation       [4] stage-2 lookahead          [5] stage-2 application
+ *   [6] host<->device copies (host entry points only)             [7] total device time
+ * (the groups printed by src/ab2rht.f90:487-490 and src/rht2ht.f90:2044-2047). */
+int paraht_ctx_phase_times(paraht_ctx ctx, double* times, int ntimes);
+/* Largest absolute entry found below the structure (r-Hessenberg / Hessenberg for A,
+ * triangular for B) before it was zeroed by the last call: [0] A, [1] B. */
+int paraht_ctx_fill_residue(paraht_ctx ctx, double* residue, int nres);
+
+/* ---- host-pointer drop-ins (copy in, reduce on the GPU, copy out) ----
+ * paraht_ab2rht  <-> ab2rht_simple(n, A, lda, B, ldb, Q, ldq, Z, ldz, nb, p, time_components)
+ *                    src/ab2rht.f90:8-13
+ * paraht_rht2ht  <-> rht2ht_householder(n, A, lda, B, ldb, Q, ldq, Z, ldz, r, nq, time_components)
+ *                    src/rht2ht.f90:1346-1351
+ * paraht_reduce  <-> the two calls in sequence, src/profilereduction.f90:136 and :144
+ * time_components is a C int (0/1) in place of the Fortran LOGICAL. */
+int paraht_ab2rht(int n, double* A, int lda, double* B, int ldb, double* Q, int ldq, double* Z, int ldz, int nb,
+                  int p, int time_components);
+int paraht_rht2ht(int n, double* A, int lda, double* B, int ldb, double* Q, int ldq, double* Z, int ldz, int r,
+                  int nq, int time_components);
+int paraht_reduce(int n, double* A, int lda, double* B, int ldb, double* Q, int ldq, double* Z, int ldz, int r,
+                  int p, int nq, int flags);
+
+/* Same, on an explicit context (host pointers). */
+int paraht_reduce_host(paraht_ctx ctx, int n, double* A, int lda, double* B, int ldb, double* Q, int ldq, double* Z,
+                       int ldz, int r, int p, int nq, int flags);
+
+/* ---- device-pointer variants: arrays already resident in device memory, no copies;
+ * work is enqueued on the context's stream and the call returns after it completes. ---- */
+int paraht_ab2rht_d(paraht_ctx ctx, int n, double* A, int lda, double* B, int ldb, double* Q, int ldq, double* Z,
+                    int ldz, int nb, int p, int flags);
+int paraht_rht2ht_d(paraht_ctx ctx, int n, double* A, int lda, double* B, int ldb, double* Q, int ldq, double* Z,
+                    int ldz, int r, int nq, int flags);
+int paraht_reduce_d(paraht_ctx ctx, int n, double* A, int lda, double* B, int ldb, double* Q, int ldq, double* Z,
+                    int ldz, int r, int p, int nq, int flags);
+
+/* ---- batched: `count` independent pencils of possibly different sizes (device pointers).
+ * Arrays of length count; r, p, nq per pencil.  No counterpart in the reference (it reduces one
+ * pencil per run); the per-pencil arithmetic is that of paraht_reduce_d. ---- */
+int paraht_reduce_batched_d(paraht_ctx ctx, int count, const int* n, double* const* A, const int* lda,
+                            double* const* B, const int* ldb, double* const* Q, const int* ldq, double* const* Z,
+                            const int* ldz, const int* r, const int* p, const int* nq, int flags);
+
+/* ---- misc ---- */
+const char* paraht_strerror(int status);
+int paraht_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PARAHT_H */

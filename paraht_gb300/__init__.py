@@ -1,0 +1,127 @@
+"""paraht_gb300 -- GB300-native two-stage Hessenberg-triangular reduction of a pencil (A, B).
+
+Python mirror of the reference's Fortran interface (same names, argument order and meaning):
+
+* ``ab2rht_simple(n, A, lda, B, ldb, Q, ldq, Z, ldz, nb, p, time_components)``
+      src/ab2rht.f90:8 -- stage 1, (A, B) -> (r-Hessenberg, triangular)
+* ``rht2ht_householder(n, A, lda, B, ldb, Q, ldq, Z, ldz, r, nq, time_components)``
+      src/rht2ht.f90:1346 -- stage 2, r-Hessenberg -> Hessenberg
+
+Arrays are numpy float64 in Fortran (column-major) order and are overwritten in place; Q and Z
+are accumulated (right-multiplied), as in the reference.  The work runs on the GPU through
+libparaht.so (C ABI in include/paraht.h); there is no CPU path.  Invalid arguments raise
+``ParahtError`` carrying the LAPACK-style negative argument index instead of silently
+producing garbage (the reference performs no checks).
+
+``Context`` exposes the device-pointer entry points (arrays resident in GPU memory), per-phase
+timings and the fill residue.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import (PARAHT_FLAG_CHECK_FINITE, PARAHT_FLAG_NO_ZERO_FILL, PARAHT_FLAG_SPLIT,
+                   PARAHT_FLAG_TIME_COMPONENTS, ParahtError, check, lib)
+
+__all__ = [
+    "ab2rht_simple", "rht2ht_householder", "reduce", "Context", "ParahtError",
+    "PARAHT_FLAG_TIME_COMPONENTS", "PARAHT_FLAG_CHECK_FINITE", "PARAHT_FLAG_SPLIT", "PARAHT_FLAG_NO_ZERO_FILL",
+]
+
+PHASE_NAMES = ("s1_genleft", "s1_genright", "s1_mul", "s2_gen", "s2_lookahead", "s2_application", "copies", "total")
+
+
+def _host_ptr(a):
+    if a is None:
+        return None
+    if not isinstance(a, np.ndarray) or a.dtype != np.float64 or not a.flags.f_contiguous:
+        raise TypeError("matrices must be Fortran-ordered float64 numpy arrays")
+    if not a.flags.writeable:
+        raise TypeError("matrices are overwritten in place and must be writeable")
+    return a.ctypes.data
+
+
+def ab2rht_simple(n, A, lda, B, ldb, Q, ldq, Z, ldz, nb, p, time_components=False):
+    """Stage 1 (src/ab2rht.f90:8-13), in place on host arrays."""
+    check(lib().paraht_ab2rht(int(n), _host_ptr(A), int(lda), _host_ptr(B), int(ldb), _host_ptr(Q), int(ldq),
+                              _host_ptr(Z), int(ldz), int(nb), int(p), int(bool(time_components))), "ab2rht_simple")
+
+
+def rht2ht_householder(n, A, lda, B, ldb, Q, ldq, Z, ldz, r, nq, time_components=False):
+    """Stage 2 (src/rht2ht.f90:1346-1351), in place on host arrays."""
+    check(lib().paraht_rht2ht(int(n), _host_ptr(A), int(lda), _host_ptr(B), int(ldb), _host_ptr(Q), int(ldq),
+                              _host_ptr(Z), int(ldz), int(r), int(nq), int(bool(time_components))),
+          "rht2ht_householder")
+
+
+def reduce(A, B, Q, Z, r, p, nq, flags=0):
+    """Both stages in sequence (src/profilereduction.f90:136, :144) on host arrays."""
+    n = A.shape[0]
+    check(lib().paraht_reduce(int(n), _host_ptr(A), A.shape[0], _host_ptr(B), B.shape[0], _host_ptr(Q), Q.shape[0],
+                              _host_ptr(Z), Z.shape[0], int(r), int(p), int(nq), int(flags)), "reduce")
+
+
+class Context:
+    """A libparaht context: one CUDA device, one stream, reusable workspace."""
+
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p()
+        check(lib().paraht_ctx_create(C.byref(self._h), int(device)), "paraht_ctx_create")
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            lib().paraht_ctx_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_ptr: int):
+        check(lib().paraht_ctx_set_stream(self._h, C.c_void_p(stream_ptr or None)), "set_stream")
+
+    # -- device pointers (ints, e.g. torch.Tensor.data_ptr()) --
+    def reduce_d(self, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, p, nq, flags=0):
+        check(lib().paraht_reduce_d(self._h, int(n), A, int(lda), B, int(ldb), Q, int(ldq), Z, int(ldz), int(r),
+                                    int(p), int(nq), int(flags)), "reduce_d")
+
+    def ab2rht_d(self, n, A, lda, B, ldb, Q, ldq, Z, ldz, nb, p, flags=0):
+        check(lib().paraht_ab2rht_d(self._h, int(n), A, int(lda), B, int(ldb), Q, int(ldq), Z, int(ldz), int(nb),
+                                    int(p), int(flags)), "ab2rht_d")
+
+    def rht2ht_d(self, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, nq, flags=0):
+        check(lib().paraht_rht2ht_d(self._h, int(n), A, int(lda), B, int(ldb), Q, int(ldq), Z, int(ldz), int(r),
+                                    int(nq), int(flags)), "rht2ht_d")
+
+    # -- host arrays on this context --
+    def reduce_host(self, A, B, Q, Z, r, p, nq, flags=0):
+        n = A.shape[0]
+        check(lib().paraht_reduce_host(self._h, int(n), _host_ptr(A), A.shape[0], _host_ptr(B), B.shape[0],
+                                       _host_ptr(Q), Q.shape[0], _host_ptr(Z), Z.shape[0], int(r), int(p), int(nq),
+                                       int(flags)), "reduce_host")
+
+    def reduce_batched_d(self, ns, As, ldas, Bs, ldbs, Qs, ldqs, Zs, ldzs, rs, ps, nqs, flags=0):
+        cnt = len(ns)
+        IA = C.c_int * cnt
+        PA = C.c_void_p * cnt
+        check(lib().paraht_reduce_batched_d(self._h, cnt, IA(*ns), PA(*As), IA(*ldas), PA(*Bs), IA(*ldbs), PA(*Qs),
+                                            IA(*ldqs), PA(*Zs), IA(*ldzs), IA(*rs), IA(*ps), IA(*nqs), int(flags)),
+              "reduce_batched_d")
+
+    def phase_times(self) -> dict:
+        buf = (C.c_double * 8)()
+        check(lib().paraht_ctx_phase_times(self._h, buf, 8), "phase_times")
+        return dict(zip(PHASE_NAMES, list(buf)))
+
+    def fill_residue(self):
+        buf = (C.c_double * 2)()
+        check(lib().paraht_ctx_fill_residue(self._h, buf, 2), "fill_residue")
+        return float(buf[0]), float(buf[1])

@@ -1,0 +1,451 @@
+// api.cu -- the extern "C" boundary of libparaht (declared in include/paraht.h).
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+
+#include "paraht_impl.h"
+#include "paraht_internal.cuh"
+
+struct paraht_ctx_s {
+  pht::Ctx c;
+  uint32_t magic;
+};
+static const uint32_t kMagic = 0x50485431u;  // "PHT1"
+
+namespace pht {
+
+void* Ctx::workspace(size_t bytes) {
+  if (bytes <= ws_bytes) return ws;
+  if (ws) {
+    cudaStreamSynchronize(stream);
+    cudaFree(ws);
+    ws = nullptr;
+    ws_bytes = 0;
+  }
+  const size_t want = bytes + bytes / 4;
+  if (cudaMalloc(&ws, want) != cudaSuccess) {
+    ws = nullptr;
+    cudaGetLastError();
+    return nullptr;
+  }
+  ws_bytes = want;
+  return ws;
+}
+
+int Ctx::ensure_staging(size_t bytes_each) {
+  if (bytes_each <= stage_bytes) return 0;
+  cudaStreamSynchronize(stream);
+  for (auto& p : stage) {
+    if (p) cudaFree(p);
+    p = nullptr;
+  }
+  stage_bytes = 0;
+  for (auto& p : stage) {
+    if (cudaMalloc(&p, bytes_each) != cudaSuccess) {
+      cudaGetLastError();
+      for (auto& q : stage) {
+        if (q) cudaFree(q);
+        q = nullptr;
+      }
+      return PARAHT_ERR_ALLOC;
+    }
+  }
+  stage_bytes = bytes_each;
+  return 0;
+}
+
+// Non-negative doubles order like their bit patterns, so the maximum of |x| can be taken with
+// an integer atomicMax.
+__global__ void k_zero_fill(int n, double* X, int ldx, int band, unsigned long long* res) {
+  const int j = blockIdx.x;
+  double m = 0.0;
+  for (int i = j + band + 1 + threadIdx.x; i < n; i += blockDim.x) {
+    double* p = X + (size_t)i + (size_t)j * ldx;
+    m = fmax(m, fabs(*p));
+    *p = 0.0;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m > 0.0) atomicMax(res, (unsigned long long)__double_as_longlong(m));
+}
+
+void zero_fill(cudaStream_t s, int n, double* A, int lda, int band, double* B, int ldb, double* dres) {
+  if (n <= 1) return;
+  cudaMemsetAsync(dres, 0, 2 * sizeof(double), s);
+  k_zero_fill<<<n, 128, 0, s>>>(n, A, lda, band, (unsigned long long*)dres);
+  k_zero_fill<<<n, 128, 0, s>>>(n, B, ldb, 0, (unsigned long long*)(dres + 1));
+}
+
+__global__ void k_check_finite(int n, const double* X, int ldx, int* flag) {
+  const int j = blockIdx.x;
+  for (int i = threadIdx.x; i < n; i += blockDim.x)
+    if (!isfinite(X[(size_t)i + (size_t)j * ldx])) atomicOr(flag, 1);
+}
+
+int check_finite(cudaStream_t s, int n, const double* A, int lda, const double* B, int ldb, int* dflag) {
+  cudaMemsetAsync(dflag, 0, sizeof(int), s);
+  k_check_finite<<<n, 256, 0, s>>>(n, A, lda, dflag);
+  k_check_finite<<<n, 256, 0, s>>>(n, B, ldb, dflag);
+  int h = 0;
+  cudaMemcpyAsync(&h, dflag, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) return PARAHT_ERR_CUDA;
+  return h ? PARAHT_ERR_NONFINITE : 0;
+}
+
+}  // namespace pht
+
+using pht::Ctx;
+
+static int ctx_ok(paraht_ctx c) { return c && c->magic == kMagic; }
+
+extern "C" int paraht_ctx_create(paraht_ctx* out, int device) {
+  if (!out) return -1;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    return PARAHT_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= ndev) return -2;
+  paraht_ctx c = new (std::nothrow) paraht_ctx_s();
+  if (!c) return PARAHT_ERR_ALLOC;
+  c->magic = kMagic;
+  Ctx& x = c->c;
+  x.device = device;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(device);
+  cudaDeviceGetAttribute(&x.max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+  cudaDeviceGetAttribute(&x.num_sms, cudaDevAttrMultiProcessorCount, device);
+  int rc = 0;
+  if (cudaStreamCreateWithFlags(&x.stream, cudaStreamNonBlocking) != cudaSuccess) rc = PARAHT_ERR_CUDA;
+  x.own_stream = true;
+  if (!rc && cudaMalloc(&x.dstatus, 64) != cudaSuccess) rc = PARAHT_ERR_ALLOC;
+  if (!rc && cudaMalloc(&x.dresidue, 2 * sizeof(double)) != cudaSuccess) rc = PARAHT_ERR_ALLOC;
+  cudaSetDevice(prev);
+  if (rc) {
+    cudaGetLastError();
+    paraht_ctx_destroy(c);
+    return rc;
+  }
+  *out = c;
+  return 0;
+}
+
+extern "C" int paraht_ctx_destroy(paraht_ctx c) {
+  if (!ctx_ok(c)) return PARAHT_ERR_BAD_CTX;
+  Ctx& x = c->c;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(x.device);
+  if (x.stream) cudaStreamSynchronize(x.stream);
+  if (x.ws) cudaFree(x.ws);
+  for (auto p : x.stage)
+    if (p) cudaFree(p);
+  if (x.dstatus) cudaFree(x.dstatus);
+  if (x.dresidue) cudaFree(x.dresidue);
+  if (x.own_stream && x.stream) cudaStreamDestroy(x.stream);
+  cudaSetDevice(prev);
+  c->magic = 0;
+  delete c;
+  return 0;
+}
+
+extern "C" int paraht_ctx_set_stream(paraht_ctx c, void* stream) {
+  if (!ctx_ok(c)) return PARAHT_ERR_BAD_CTX;
+  Ctx& x = c->c;
+  if (stream) {
+    if (x.own_stream && x.stream) {
+      cudaStreamSynchronize(x.stream);
+      cudaStreamDestroy(x.stream);
+    }
+    x.stream = (cudaStream_t)stream;
+    x.own_stream = false;
+  } else if (!x.own_stream) {
+    if (cudaStreamCreateWithFlags(&x.stream, cudaStreamNonBlocking) != cudaSuccess) return PARAHT_ERR_CUDA;
+    x.own_stream = true;
+  }
+  return 0;
+}
+
+extern "C" int paraht_ctx_phase_times(paraht_ctx c, double* t, int nt) {
+  if (!ctx_ok(c)) return PARAHT_ERR_BAD_CTX;
+  if (!t && nt > 0) return -2;
+  for (int i = 0; i < nt && i < 8; ++i) t[i] = c->c.phase[i];
+  for (int i = 8; i < nt; ++i) t[i] = 0.0;
+  return 0;
+}
+
+extern "C" int paraht_ctx_fill_residue(paraht_ctx c, double* r, int nr) {
+  if (!ctx_ok(c)) return PARAHT_ERR_BAD_CTX;
+  for (int i = 0; i < nr && i < 2; ++i) r[i] = c->c.residue[i];
+  return 0;
+}
+
+// Argument checks in LAPACK INFO style; `off` shifts the index for entry points with a leading
+// ctx argument.  which: 1 = stage 1 (r, p), 2 = stage 2 (r, nq), 3 = both (r, p, nq).
+static int check_args(int which, int off, int n, const double* A, int lda, const double* B, int ldb, const double* Q,
+                      int ldq, const double* Z, int ldz, int r, int p, int nq) {
+  if (n < 0) return -(1 + off);
+  const int ldmin = std::max(1, n);
+  if (n > 0 && !A) return -(2 + off);
+  if (lda < ldmin) return -(3 + off);
+  if (n > 0 && !B) return -(4 + off);
+  if (ldb < ldmin) return -(5 + off);
+  if (n > 0 && !Q) return -(6 + off);
+  if (ldq < ldmin) return -(7 + off);
+  if (n > 0 && !Z) return -(8 + off);
+  if (ldz < ldmin) return -(9 + off);
+  if (r < 1 || r > 64) return -(10 + off);
+  if (which == 1 && p < 2) return -(11 + off);
+  if (which == 2 && (nq < 1 || nq > r)) return -(11 + off);
+  if (which == 3) {
+    if (p < 2) return -(11 + off);
+    if (nq < 1 || nq > r) return -(12 + off);
+  }
+  return 0;
+}
+
+static int finish(Ctx& x) {
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(x.stream);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return PARAHT_ERR_CUDA;
+  }
+  return 0;
+}
+
+// Runs the selected stages on device-resident arrays (stream-ordered; caller synchronises).
+static int run_device(Ctx& x, int which, int n, double* A, int lda, double* B, int ldb, double* Q, int ldq, double* Z,
+                      int ldz, int r, int p, int nq, int flags) {
+  if (n == 0) return 0;
+  if (flags & PARAHT_FLAG_SPLIT) return PARAHT_ERR_NOT_SUPPORTED;
+  const bool timed = flags & PARAHT_FLAG_TIME_COMPONENTS;
+  if (flags & PARAHT_FLAG_CHECK_FINITE) {
+    const int rc = pht::check_finite(x.stream, n, A, lda, B, ldb, x.dstatus);
+    if (rc) return rc;
+  }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (timed) {
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, x.stream);
+  }
+  int rc = 0;
+  if (which & 1) {
+    x.timer.reset(0);
+    rc = pht::s1_run(x, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, p, timed ? &x.timer : nullptr);
+    if (!rc && timed) {
+      rc = finish(x);
+      x.timer.accumulate(x.phase, 8);
+    }
+  }
+  if (!rc && (which & 2)) {
+    x.timer.reset(3);
+    rc = pht::s2_run(x, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, nq, timed ? &x.timer : nullptr);
+    if (!rc && timed) {
+      rc = finish(x);
+      x.timer.accumulate(x.phase, 8);
+    }
+  }
+  if (!rc && !(flags & PARAHT_FLAG_NO_ZERO_FILL)) {
+    pht::zero_fill(x.stream, n, A, lda, (which & 2) ? 1 : r, B, ldb, x.dresidue);
+    cudaMemcpyAsync(x.residue, x.dresidue, 2 * sizeof(double), cudaMemcpyDeviceToHost, x.stream);
+  }
+  if (timed) {
+    cudaEventRecord(e1, x.stream);
+    if (!rc) rc = finish(x);
+    float ms = 0;
+    if (!rc && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess) x.phase[7] = ms * 1e-3;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+  return rc;
+}
+
+static int device_entry(paraht_ctx c, int which, int n, double* A, int lda, double* B, int ldb, double* Q, int ldq,
+                        double* Z, int ldz, int r, int p, int nq, int flags) {
+  if (!ctx_ok(c)) return PARAHT_ERR_BAD_CTX;
+  Ctx& x = c->c;
+  int rc = check_args(which, 1, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, p, nq);
+  if (rc) return rc;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(x.device);
+  for (double& v : x.phase) v = 0.0;
+  x.residue[0] = x.residue[1] = 0.0;
+  rc = run_device(x, which, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, p, nq, flags);
+  if (!rc) rc = finish(x);
+  cudaSetDevice(prev);
+  return rc;
+}
+
+extern "C" int paraht_ab2rht_d(paraht_ctx c, int n, double* A, int lda, double* B, int ldb, double* Q, int ldq,
+                               double* Z, int ldz, int nb, int p, int flags) {
+  return device_entry(c, 1, n, A, lda, B, ldb, Q, ldq, Z, ldz, nb, p, 1, flags);
+}
+extern "C" int paraht_rht2ht_d(paraht_ctx c, int n, double* A, int lda, double* B, int ldb, double* Q, int ldq,
+                               double* Z, int ldz, int r, int nq, int flags) {
+  return device_entry(c, 2, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, 2, nq, flags);
+}
+extern "C" int paraht_reduce_d(paraht_ctx c, int n, double* A, int lda, double* B, int ldb, double* Q, int ldq,
+                               double* Z, int ldz, int r, int p, int nq, int flags) {
+  return device_entry(c, 3, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, p, nq, flags);
+}
+
+// Host-pointer path: stage the four matrices into the context's device buffers, reduce, copy
+// back.  `off` is the argument-index offset (0 for context-free entry points).
+static int host_entry(paraht_ctx c, int off, int which, int n, double* A, int lda, double* B, int ldb, double* Q,
+                      int ldq, double* Z, int ldz, int r, int p, int nq, int flags) {
+  if (!ctx_ok(c)) return PARAHT_ERR_BAD_CTX;
+  Ctx& x = c->c;
+  int rc = check_args(which, off, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, p, nq);
+  if (rc || n == 0) return rc;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(x.device);
+  for (double& v : x.phase) v = 0.0;
+  x.residue[0] = x.residue[1] = 0.0;
+  const int ldd = (n + 3) & ~3;  // 32-byte aligned columns on the device
+  rc = x.ensure_staging((size_t)ldd * n * sizeof(double));
+  if (!rc) {
+    double* h[4] = {A, B, Q, Z};
+    const int ld[4] = {lda, ldb, ldq, ldz};
+    cudaEvent_t c0, c1, c2, c3;
+    cudaEventCreate(&c0);
+    cudaEventCreate(&c1);
+    cudaEventCreate(&c2);
+    cudaEventCreate(&c3);
+    cudaEventRecord(c0, x.stream);
+    for (int i = 0; i < 4; ++i)
+      cudaMemcpy2DAsync(x.stage[i], (size_t)ldd * sizeof(double), h[i], (size_t)ld[i] * sizeof(double),
+                        (size_t)n * sizeof(double), n, cudaMemcpyHostToDevice, x.stream);
+    cudaEventRecord(c1, x.stream);
+    rc = run_device(x, which, n, x.stage[0], ldd, x.stage[1], ldd, x.stage[2], ldd, x.stage[3], ldd, r, p, nq, flags);
+    cudaEventRecord(c2, x.stream);
+    if (!rc)
+      for (int i = 0; i < 4; ++i)
+        cudaMemcpy2DAsync(h[i], (size_t)ld[i] * sizeof(double), x.stage[i], (size_t)ldd * sizeof(double),
+                          (size_t)n * sizeof(double), n, cudaMemcpyDeviceToHost, x.stream);
+    cudaEventRecord(c3, x.stream);
+    const int rc2 = finish(x);
+    if (!rc) rc = rc2;
+    if (!rc) {
+      float a = 0, b = 0;
+      cudaEventElapsedTime(&a, c0, c1);
+      cudaEventElapsedTime(&b, c2, c3);
+      x.phase[6] = (a + b) * 1e-3;
+    }
+    cudaEventDestroy(c0);
+    cudaEventDestroy(c1);
+    cudaEventDestroy(c2);
+    cudaEventDestroy(c3);
+  }
+  cudaSetDevice(prev);
+  return rc;
+}
+
+extern "C" int paraht_reduce_host(paraht_ctx c, int n, double* A, int lda, double* B, int ldb, double* Q, int ldq,
+                                  double* Z, int ldz, int r, int p, int nq, int flags) {
+  return host_entry(c, 1, 3, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, p, nq, flags);
+}
+
+// One lazily created context per host thread for the context-free drop-ins.
+static thread_local paraht_ctx tl_ctx = nullptr;
+static thread_local int tl_dev = -1;
+static int default_ctx(paraht_ctx* out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return PARAHT_ERR_NO_DEVICE;
+  }
+  if (tl_ctx && tl_dev != dev) {
+    paraht_ctx_destroy(tl_ctx);
+    tl_ctx = nullptr;
+  }
+  if (!tl_ctx) {
+    const int rc = paraht_ctx_create(&tl_ctx, dev);
+    if (rc) return rc;
+    tl_dev = dev;
+  }
+  *out = tl_ctx;
+  return 0;
+}
+
+extern "C" int paraht_ab2rht(int n, double* A, int lda, double* B, int ldb, double* Q, int ldq, double* Z, int ldz,
+                             int nb, int p, int time_components) {
+  if (const int bad = check_args(1, 0, n, A, lda, B, ldb, Q, ldq, Z, ldz, nb, p, 1)) return bad;
+  if (n == 0) return 0;
+  paraht_ctx c;
+  const int rc = default_ctx(&c);
+  if (rc) return rc;
+  return host_entry(c, 0, 1, n, A, lda, B, ldb, Q, ldq, Z, ldz, nb, p, 1,
+                    time_components ? PARAHT_FLAG_TIME_COMPONENTS : 0);
+}
+extern "C" int paraht_rht2ht(int n, double* A, int lda, double* B, int ldb, double* Q, int ldq, double* Z, int ldz,
+                             int r, int nq, int time_components) {
+  if (const int bad = check_args(2, 0, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, 2, nq)) return bad;
+  if (n == 0) return 0;
+  paraht_ctx c;
+  const int rc = default_ctx(&c);
+  if (rc) return rc;
+  return host_entry(c, 0, 2, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, 2, nq,
+                    time_components ? PARAHT_FLAG_TIME_COMPONENTS : 0);
+}
+extern "C" int paraht_reduce(int n, double* A, int lda, double* B, int ldb, double* Q, int ldq, double* Z, int ldz,
+                             int r, int p, int nq, int flags) {
+  if (const int bad = check_args(3, 0, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, p, nq)) return bad;
+  if (n == 0) return 0;
+  paraht_ctx c;
+  const int rc = default_ctx(&c);
+  if (rc) return rc;
+  return host_entry(c, 0, 3, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, p, nq, flags);
+}
+
+extern "C" int paraht_reduce_batched_d(paraht_ctx c, int count, const int* n, double* const* A, const int* lda,
+                                       double* const* B, const int* ldb, double* const* Q, const int* ldq,
+                                       double* const* Z, const int* ldz, const int* r, const int* p, const int* nq,
+                                       int flags) {
+  if (!ctx_ok(c)) return PARAHT_ERR_BAD_CTX;
+  if (count < 0) return -2;
+  if (count > 0 && (!n || !A || !lda || !B || !ldb || !Q || !ldq || !Z || !ldz || !r || !p || !nq)) return -3;
+  for (int i = 0; i < count; ++i) {
+    const int rc = check_args(3, 0, n[i], A[i], lda[i], B[i], ldb[i], Q[i], ldq[i], Z[i], ldz[i], r[i], p[i], nq[i]);
+    if (rc) return -3;
+  }
+  for (int i = 0; i < count; ++i) {
+    const int rc = paraht_reduce_d(c, n[i], A[i], lda[i], B[i], ldb[i], Q[i], ldq[i], Z[i], ldz[i], r[i], p[i], nq[i],
+                                   flags & ~PARAHT_FLAG_TIME_COMPONENTS);
+    if (rc) return rc;
+  }
+  return 0;
+}
+
+extern "C" const char* paraht_strerror(int s) {
+  switch (s) {
+    case PARAHT_OK:
+      return "success";
+    case PARAHT_ERR_CUDA:
+      return "CUDA runtime error";
+    case PARAHT_ERR_ALLOC:
+      return "allocation failed";
+    case PARAHT_ERR_TIMEOUT:
+      return "device-side wait timed out";
+    case PARAHT_ERR_NONFINITE:
+      return "non-finite input";
+    case PARAHT_ERR_NOT_SUPPORTED:
+      return "not supported";
+    case PARAHT_ERR_NO_DEVICE:
+      return "no CUDA device";
+    case PARAHT_ERR_BAD_CTX:
+      return "invalid context";
+    default:
+      return s < 0 && s >= -20 ? "invalid argument" : "unknown status";
+  }
+}
+
+extern "C" int paraht_version(void) { return PARAHT_VERSION; }

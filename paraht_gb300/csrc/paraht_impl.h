@@ -1,0 +1,77 @@
+// paraht_impl.h -- host-side internals shared by the stage drivers and the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "../../include/paraht.h"
+
+namespace pht {
+
+// Records CUDA events at phase boundaries; per-phase device time is accumulated after the
+// stream has finished.  mark(s, p) starts phase p (p < 0 ends the current phase).
+struct PhaseTimer {
+  std::vector<cudaEvent_t> ev;
+  std::vector<int> phase;
+  size_t used = 0;
+  int offset = 0;  // phase index offset (stage 2 phases start at 3)
+  void reset(int off) {
+    used = 0;
+    phase.clear();
+    offset = off;
+  }
+  void mark(cudaStream_t s, int p) {
+    if (used == ev.size()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      ev.push_back(e);
+    }
+    cudaEventRecord(ev[used], s);
+    phase.push_back(p < 0 ? -1 : p + offset);
+    ++used;
+  }
+  // Adds the elapsed times into out[0..nout) (call after the stream completed).
+  void accumulate(double* out, int nout) {
+    for (size_t i = 1; i < used; ++i) {
+      const int p = phase[i - 1];
+      if (p < 0 || p >= nout) continue;
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, ev[i - 1], ev[i]) == cudaSuccess) out[p] += ms * 1e-3;
+    }
+  }
+  ~PhaseTimer() {
+    for (auto e : ev) cudaEventDestroy(e);
+  }
+};
+
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int max_smem = 0;
+  int num_sms = 0;
+  void* ws = nullptr;  // workspace (grown on demand, reused across calls)
+  size_t ws_bytes = 0;
+  double* stage[4] = {nullptr, nullptr, nullptr, nullptr};  // device copies for host entries
+  size_t stage_bytes = 0;
+  int* dstatus = nullptr;  // device status word
+  PhaseTimer timer;
+  double phase[8] = {0};
+  double residue[2] = {0};
+  double* dresidue = nullptr;
+  void* workspace(size_t bytes);
+  int ensure_staging(size_t bytes_each);
+};
+
+size_t s1_workspace_bytes(int n, int nb, int p);
+size_t s2_workspace_bytes(int n, int r, int nq);
+int s1_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, int ldq, double* Z, int ldz, int nb,
+           int p, PhaseTimer* timer);
+int s2_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, int ldq, double* Z, int ldz, int r,
+           int nq, PhaseTimer* timer);
+// Zeroes entries below the structure (lower bandwidth `band` for A, 0 for B) and records the
+// largest absolute value zeroed in dres[0] (A) and dres[1] (B).
+void zero_fill(cudaStream_t s, int n, double* A, int lda, int band, double* B, int ldb, double* dres);
+int check_finite(cudaStream_t s, int n, const double* A, int lda, const double* B, int ldb, int* dflag);
+
+}  // namespace pht

@@ -1,0 +1,89 @@
+// paraht_internal.cuh -- shared device helpers and launch geometry for the ParaHT GB300 library.
+//
+// Conventions
+//   * Matrices are column-major FP64 with a leading dimension (as in the reference, whose
+//     arrays are Fortran A(lda,*)).  Device code uses 0-based indices; comments that cite the
+//     reference use its 1-based indices.
+//   * A compact-WY "op" is one block reflector H = I - V T V^T with V stored column-wise and
+//     explicitly (unit diagonal and the zeros above it are stored), T k x k.  Left ops apply
+//     H^T from the left to a row range of a matrix (dlarfb 'L','T'); right ops apply H from the
+//     right to a column range (dlarfb 'R','N').  Row-wise reflectors (LQ/RQ) are stored
+//     transposed so that they are column-wise too.
+//   * Every bulk update of both stages is a sequence of such ops applied in a fixed order; the
+//     order matters where ops overlap and follows the reference's loop order.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define PHT_DEV __device__ __forceinline__
+
+namespace pht {
+
+constexpr int kWarp = 32;
+
+// ---------------------------------------------------------------------------------------
+// CTA-wide sum of one double per thread; every thread receives the total.
+// `red` must hold at least blockDim.x/32 doubles of shared memory.
+// ---------------------------------------------------------------------------------------
+PHT_DEV double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+PHT_DEV double block_sum(double v, double* red) {
+  v = warp_sum(v);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+  __syncthreads();  // red may still be read by a previous call
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  double s = (l < nw) ? red[l] : 0.0;
+  s = warp_sum(s);
+  return s;
+}
+
+// Householder generation with the semantics of LAPACK DLARFG: given alpha and the squared norm
+// of x, returns tau and the scale factor 1/(alpha-beta) for x; beta replaces alpha.
+// Computed redundantly by every thread from identical inputs (bitwise identical results), so no
+// broadcast is needed.  tau = 0 (identity) when x == 0, as in DLARFG.
+struct Reflector {
+  double tau, scal, beta;
+};
+PHT_DEV Reflector make_reflector(double alpha, double xnorm2) {
+  Reflector h;
+  if (xnorm2 == 0.0) {
+    h.tau = 0.0;
+    h.scal = 1.0;
+    h.beta = alpha;
+    return h;
+  }
+  const double xnorm = sqrt(xnorm2);
+  const double beta = -copysign(hypot(alpha, xnorm), alpha);
+  h.tau = (beta - alpha) / beta;
+  h.scal = 1.0 / (alpha - beta);
+  h.beta = beta;
+  return h;
+}
+
+// ---------------------------------------------------------------------------------------
+// Compact-WY op descriptors.
+// ---------------------------------------------------------------------------------------
+struct WYOp {
+  int start;  // first row (left op) / first column (right op) of the reflector span
+  int len;    // length of the span (rows of V)
+  int k;      // number of reflectors (columns of V)
+  int lo;     // first column (left op) / first row (right op) that the op touches
+  int hi;     // last column (left op) / last row (right op), inclusive
+  const double* V;  // len x k, column-major, leading dimension ldv
+  int ldv;
+  const double* T;  // k x k, column-major, leading dimension ldt
+  int ldt;
+};
+
+}  // namespace pht
+
+// Status word written by device code (bounded waits, argument checks).
+struct PhtDeviceStatus {
+  int code;
+  int where;
+};

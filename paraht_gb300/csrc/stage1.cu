@@ -1,0 +1,488 @@
+// stage1.cu -- stage 1 of the HT reduction on the GPU: (A general, B upper triangular) ->
+// (A r-Hessenberg, B upper triangular), accumulating Q <- Q*Q1 and Z <- Z*Z1.
+//
+// Follows src/ab2rht.f90:8-495 (ab2rht_simple).  Per panel jb (ab2rht.f90:71):
+//   1. k_s1_left_gen      QR of the overlapping p*nb x nb blocks of the panel, bottom to top
+//                         (ab2rht.f90:85-123): reflectors VL, triangular factors TL, R into A.
+//   2. left ops on B, A and right ops on Q with (VL, TL) (ab2rht.f90:135-250), all blocks in
+//      bottom-to-top order, as ordered compact-WY op lists (wy_apply.cuh).
+//   3. per block, bottom to top: k_s1_right_gen computes the RQ of the diagonal L x L block of B,
+//      the first nb rows of its orthogonal factor and their LQ (the "RQ->LQ trick",
+//      ab2rht.f90:282-312) giving nb right reflectors (VR, TR); they are applied at once to every
+//      row of B above the block's last row (ab2rht.f90:317-367) and the first nb columns of the
+//      block are zeroed below the diagonal (ab2rht.f90:329-333).
+//   4. right ops on A and Z with (VR, TR), all blocks in order (ab2rht.f90:387-467).
+// The arithmetic is FP64 throughout.
+#include <algorithm>
+
+#include "paraht_internal.cuh"
+#include "paraht_impl.h"
+#include "wy_apply.cuh"
+
+namespace pht {
+
+// ------------------------------------------------------------------------------------------
+// Panel geometry (0-based).  Block o (o = 0 .. nblocks-1) is the o-th block from the bottom.
+// ------------------------------------------------------------------------------------------
+struct S1Panel {
+  int n, nb, p, jb0;  // jb0: first panel column (0-based)
+  int nblocks, ibtop0, stride, L;
+  PHT_DEV __host__ int ib(int o) const { return ibtop0 - o * stride; }
+  PHT_DEV __host__ int ib2(int o) const { return min(n - 1, ib(o) + L - 1); }
+  PHT_DEV __host__ int nb2(int o) const { return ib2(o) - ib(o) + 1; }
+};
+
+static S1Panel make_panel(int n, int nb, int p, int jb0) {
+  S1Panel g;
+  g.n = n;
+  g.nb = nb;
+  g.p = p;
+  g.jb0 = jb0;
+  const int m = n - nb - jb0;  // rows jb0+nb .. n-1  (ab2rht.f90:74: n-nb-jb+1 with 1-based jb)
+  g.stride = (p - 1) * nb;
+  g.nblocks = (m + g.stride - 1) / g.stride;
+  g.L = p * nb;
+  g.ibtop0 = jb0 + nb + (g.nblocks - 1) * g.stride;
+  return g;
+}
+
+// Left ops of the panel on B (columns >= ib) or A (columns >= jb+nb): dlarfb('L','T','F','C').
+struct GeoS1Left {
+  S1Panel P;
+  const double* VL;
+  const double* TL;
+  int onA;
+  PHT_DEV int count() const { return P.nblocks; }
+  PHT_DEV WYOp op(int o) const {
+    WYOp w;
+    w.start = P.ib(o);
+    w.len = P.nb2(o);
+    w.k = min(P.nb, w.len);
+    w.lo = onA ? P.jb0 + P.nb : P.ib(o);
+    w.hi = P.n - 1;
+    w.V = VL + (size_t)o * P.L * P.nb;
+    w.ldv = P.L;
+    w.T = TL + (size_t)o * P.nb * P.nb;
+    w.ldt = P.nb;
+    return w;
+  }
+};
+
+// Right ops of the panel's left reflectors on Q: Q(:, ib:ib2) <- Q H (ab2rht.f90:241).
+struct GeoS1Q {
+  S1Panel P;
+  const double* VL;
+  const double* TL;
+  PHT_DEV int count() const { return P.nblocks; }
+  PHT_DEV WYOp op(int o) const {
+    WYOp w;
+    w.start = P.ib(o);
+    w.len = P.nb2(o);
+    w.k = min(P.nb, w.len);
+    w.lo = 0;
+    w.hi = P.n - 1;
+    w.V = VL + (size_t)o * P.L * P.nb;
+    w.ldv = P.L;
+    w.T = TL + (size_t)o * P.nb * P.nb;
+    w.ldt = P.nb;
+    return w;
+  }
+};
+
+// Right reflectors (stored transposed in VRc) on A, Z (all rows) or on B (rows up to ib2 of a
+// single block, bl_only >= 0).
+struct GeoS1Right {
+  S1Panel P;
+  const double* VRc;
+  const double* TR;
+  int bl_only;  // -1: all blocks, all rows; else only block bl_only, rows [0, ib2]
+  PHT_DEV int count() const { return bl_only >= 0 ? 1 : P.nblocks; }
+  PHT_DEV WYOp op(int i) const {
+    const int o = bl_only >= 0 ? bl_only : i;
+    WYOp w;
+    w.start = P.ib(o);
+    w.len = P.nb2(o);
+    w.k = (w.len > P.nb) ? P.nb : w.len;
+    w.lo = 0;
+    w.hi = bl_only >= 0 ? P.ib2(o) : P.n - 1;
+    w.V = VRc + (size_t)o * P.L * P.nb;
+    w.ldv = P.L;
+    w.T = TR + (size_t)o * P.nb * P.nb;
+    w.ldt = P.nb;
+    return w;
+  }
+};
+
+// ------------------------------------------------------------------------------------------
+// Triangular factor of a block reflector from the Gram matrix of its vectors:
+//   forward  (dlarft 'F'): T upper, T[l][m] = -tau_m * sum_{q=l}^{m-1} T[l][q] G[q][m]
+//   backward (dlarft 'B'): T lower, T[m][i] = -tau_i * sum_{l=i+1}^{m} T[m][l] G[l][i]
+// G (k x k, ld kg, only the needed triangle) and tau live in shared memory; T is written to
+// global memory (ld ldt) with explicit zeros in the unused triangle.  Columns are generated
+// one after the other (the recurrence is sequential in m); rows within a column in parallel.
+// ------------------------------------------------------------------------------------------
+__device__ void form_t_forward(int k, const double* G, int kg, const double* tau, double* Ts, int nbT, double* T,
+                               int ldt) {
+  // Ts: shared scratch nbT x nbT (ld nbT)
+  const int t = threadIdx.x;
+  for (int e = t; e < nbT * nbT; e += blockDim.x) Ts[e] = 0.0;
+  __syncthreads();
+  for (int m = 0; m < k; ++m) {
+    if (t < m) {
+      double s = 0.0;
+      for (int q = t; q < m; ++q) s = fma(Ts[t + q * nbT], G[q + m * kg], s);
+      Ts[t + m * nbT] = -tau[m] * s;
+    }
+    if (t == m) Ts[m + m * nbT] = tau[m];
+    __syncthreads();
+  }
+  for (int e = t; e < nbT * nbT; e += blockDim.x) T[(e % nbT) + (size_t)(e / nbT) * ldt] = Ts[e];
+}
+
+__device__ void form_t_backward(int k, const double* G, int kg, const double* tau, double* Ts, int nbT, double* T,
+                                int ldt) {
+  const int t = threadIdx.x;
+  for (int e = t; e < nbT * nbT; e += blockDim.x) Ts[e] = 0.0;
+  __syncthreads();
+  for (int i = k - 1; i >= 0; --i) {
+    if (t == i) Ts[i + i * nbT] = tau[i];
+    if (t > i && t < k) {
+      double s = 0.0;
+      for (int l = i + 1; l <= t; ++l) s = fma(Ts[t + l * nbT], G[l + i * kg], s);
+      Ts[t + i * nbT] = -tau[i] * s;
+    }
+    __syncthreads();
+  }
+  for (int e = t; e < nbT * nbT; e += blockDim.x) T[(e % nbT) + (size_t)(e / nbT) * ldt] = Ts[e];
+}
+
+// ------------------------------------------------------------------------------------------
+// Left generation (ab2rht.f90:85-123): for each block bottom to top, Householder QR
+// (dgeqr2 semantics) of A(ib:ib2, jb:jb+nb-1); store VL explicitly (unit diagonal, zeros
+// above), write R (zeros below) back to A, form TL (dlarft 'F','C').
+// Shared memory: P tile (L x nb, ld L+1) + G (nb x nb) + Ts (nb x nb) + tau (nb) + reduction.
+// ------------------------------------------------------------------------------------------
+constexpr int kGenThreads = 256;
+
+__global__ void __launch_bounds__(kGenThreads) k_s1_left_gen(double* __restrict__ A, int lda, S1Panel P,
+                                                             double* __restrict__ VL, double* __restrict__ TL) {
+  extern __shared__ double sm[];
+  const int L = P.L, nb = P.nb, ldp = L + 1;
+  double* Pt = sm;                    // ldp * nb
+  double* G = Pt + (size_t)ldp * nb;  // nb*nb
+  double* Ts = G + nb * nb;           // nb*nb
+  double* tau = Ts + nb * nb;         // nb
+  double* red = tau + nb;             // 32
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5, nwarp = blockDim.x >> 5;
+  const int jb0 = P.jb0;
+  for (int o = 0; o < P.nblocks; ++o) {
+    const int ib0 = P.ib(o), nb2 = P.nb2(o), k = min(nb, nb2);
+    for (int e = t; e < nb2 * nb; e += blockDim.x) {
+      const int i = e % nb2, j = e / nb2;
+      Pt[i + j * ldp] = A[(size_t)(ib0 + i) + (size_t)(jb0 + j) * lda];
+    }
+    __syncthreads();
+    for (int j = 0; j < k; ++j) {
+      double part = 0.0;
+      for (int i = j + 1 + t; i < nb2; i += blockDim.x) part = fma(Pt[i + j * ldp], Pt[i + j * ldp], part);
+      const double ss = block_sum(part, red);
+      const Reflector h = make_reflector(Pt[j + j * ldp], ss);
+      __syncthreads();  // everyone has read alpha
+      for (int i = j + 1 + t; i < nb2; i += blockDim.x) Pt[i + j * ldp] *= h.scal;
+      __syncthreads();
+      if (h.tau != 0.0) {
+        for (int c = j + 1 + warp; c < nb; c += nwarp) {
+          double s = (lane == 0) ? Pt[j + c * ldp] : 0.0;
+          for (int i = j + 1 + lane; i < nb2; i += 32) s = fma(Pt[i + j * ldp], Pt[i + c * ldp], s);
+          const double tw = h.tau * warp_sum(s);
+          if (lane == 0) Pt[j + c * ldp] -= tw;
+          for (int i = j + 1 + lane; i < nb2; i += 32) Pt[i + c * ldp] = fma(-tw, Pt[i + j * ldp], Pt[i + c * ldp]);
+        }
+      }
+      __syncthreads();
+      if (t == 0) {
+        Pt[j + j * ldp] = h.beta;
+        tau[j] = h.tau;
+      }
+      __syncthreads();
+    }
+    for (int j = k + t; j < nb; j += blockDim.x) tau[j] = 0.0;
+    // VL (explicit), and R / zeros back into A.
+    double* V = VL + (size_t)o * L * nb;
+    for (int e = t; e < L * nb; e += blockDim.x) {
+      const int i = e % L, j = e / L;
+      double v = 0.0;
+      if (j < k && i < nb2) v = (i > j) ? Pt[i + j * ldp] : (i == j ? 1.0 : 0.0);
+      V[i + (size_t)j * L] = v;
+    }
+    for (int e = t; e < nb2 * nb; e += blockDim.x) {
+      const int i = e % nb2, j = e / nb2;
+      A[(size_t)(ib0 + i) + (size_t)(jb0 + j) * lda] = (i <= j) ? Pt[i + j * ldp] : 0.0;
+    }
+    // Gram matrix G[q][m] = v_q . v_m  (q < m < k), v explicit: unit at row q.
+    for (int e = t; e < nb * nb; e += blockDim.x) {
+      const int q = e % nb, m = e / nb;
+      double s = 0.0;
+      if (q < m && m < k) {
+        s = Pt[m + q * ldp];  // v_q[m] * v_m[m] (= 1)
+        for (int i = m + 1; i < nb2; ++i) s = fma(Pt[i + q * ldp], Pt[i + m * ldp], s);
+      }
+      G[q + m * nb] = s;
+    }
+    __syncthreads();
+    form_t_forward(k, G, nb, tau, Ts, nb, TL + (size_t)o * nb * nb, nb);
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Right generation for one block (ab2rht.f90:282-312).  S <- B(ib:ib2, ib:ib2) (nb2 x nb2);
+// RQ (dgerq2 semantics, rows bottom to top, reflector for row i stored in S(i, 0:i-1) with an
+// implicit unit at column i).  If nb2 > nb: M <- first nb rows of the orthogonal factor
+// H(1)...H(nb2) (dorgrq), then LQ of M (dgelq2) -> nb forward row-wise reflectors, T forward
+// (dlarft 'F','R').  Else: the nb2 RQ reflectors themselves, T backward (dlarft 'B','R').
+// VRc (block o) receives the reflectors transposed (column-wise, L x nb), TR the T factor.
+// Shared memory: S (nb2 x nb2, ld L+1), M (nb x L), partial sums, G, Ts, tau.
+// ------------------------------------------------------------------------------------------
+constexpr int kRgenThreads = 512;
+
+__global__ void __launch_bounds__(kRgenThreads) k_s1_right_gen(const double* __restrict__ B, int ldb, S1Panel P, int o,
+                                                               double* __restrict__ VRc, double* __restrict__ TR,
+                                                               double* __restrict__ gscratch) {
+  extern __shared__ double sm[];
+  const int L = P.L, nb = P.nb, lds = L + 1;
+  const int ib0 = P.ib(o), nb2 = P.nb2(o);
+  const int t = threadIdx.x, nt = blockDim.x;
+  // S in shared memory when it fits, else in global scratch (same code path).
+  double* tauR = sm;                      // L
+  double* tauL = tauR + L;                // nb
+  double* G = tauL + nb;                  // nb*nb
+  double* Ts = G + nb * nb;               // nb*nb
+  double* red = Ts + nb * nb;             // 32
+  double* part = red + 32;                // kRgenThreads partial sums
+  double* S = part + kRgenThreads;        // (L+1)*L when it fits in shared memory
+  double* M = S + (size_t)lds * L;        // nb * (L+1)
+  if (gscratch) {
+    S = gscratch;
+    M = gscratch + (size_t)lds * L;
+  }
+  const int ldm = nb;  // M is nb x nb2, column-major with ld nb: M[r + c*nb]
+  for (int e = t; e < nb2 * nb2; e += nt) {
+    const int i = e % nb2, j = e / nb2;
+    S[i + j * lds] = B[(size_t)(ib0 + i) + (size_t)(ib0 + j) * ldb];
+  }
+  __syncthreads();
+  // ---- RQ, rows bottom to top ----
+  const int nq4 = 4;
+  for (int i = nb2 - 1; i >= 0; --i) {
+    double ps = 0.0;
+    for (int c = t; c < i; c += nt) ps = fma(S[i + c * lds], S[i + c * lds], ps);
+    const double ss = block_sum(ps, red);
+    const Reflector h = make_reflector(S[i + i * lds], ss);
+    __syncthreads();
+    for (int c = t; c < i; c += nt) S[i + c * lds] *= h.scal;
+    __syncthreads();
+    if (h.tau != 0.0 && i > 0) {
+      // rows rho < i: w = S[rho][i] + sum_{c<i} S[rho][c] v_c
+      const int rows_per_pass = nt / nq4;
+      for (int rho0 = 0; rho0 < i; rho0 += rows_per_pass) {
+        const int lr = t % rows_per_pass, rho = rho0 + lr, qq = t / rows_per_pass;
+        const int cpart = (i + nq4 - 1) / nq4;
+        const int c0 = qq * cpart, c1 = min(i, c0 + cpart);
+        double s = 0.0;
+        if (rho < i)
+          for (int c = c0; c < c1; ++c) s = fma(S[rho + c * lds], S[i + c * lds], s);
+        part[qq * rows_per_pass + lr] = s;
+        __syncthreads();
+        if (rho < i) {
+          const double w = S[rho + i * lds] + ((part[lr] + part[rows_per_pass + lr]) +
+                                               (part[2 * rows_per_pass + lr] + part[3 * rows_per_pass + lr]));
+          const double tw = h.tau * w;
+          for (int c = c0; c < c1; ++c) S[rho + c * lds] = fma(-tw, S[i + c * lds], S[rho + c * lds]);
+          if (qq == 0) S[rho + i * lds] -= tw;
+        }
+        __syncthreads();
+      }
+    }
+    if (t == 0) {
+      S[i + i * lds] = h.beta;
+      tauR[i] = h.tau;
+    }
+    __syncthreads();
+  }
+  double* V = VRc + (size_t)o * L * nb;
+  double* Tout = TR + (size_t)o * nb * nb;
+  if (nb2 > nb) {
+    // ---- M = [I 0] H(1) H(2) ... H(nb2)  (first nb rows of the RQ orthogonal factor) ----
+    for (int e = t; e < nb * nb2; e += nt) {
+      const int r = e % nb, c = e / nb;
+      M[r + c * ldm] = (r == c) ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    for (int i = 0; i < nb2; ++i) {
+      const double ti = tauR[i];
+      if (ti != 0.0) {
+        // row r of M: w = sum_{c<=i} M[r][c] v_c ; v_i = 1
+        const int ng = nt / nb;  // groups per row
+        const int r = t % nb, g = t / nb;
+        const int cpart = (i + 1 + ng - 1) / ng;
+        const int c0 = g * cpart, c1 = min(i + 1, c0 + cpart);
+        double s = 0.0;
+        for (int c = c0; c < c1; ++c) s = fma(M[r + c * ldm], (c == i) ? 1.0 : S[i + c * lds], s);
+        if (g < ng) part[g * nb + r] = s;
+        __syncthreads();
+        double w = 0.0;
+        for (int gg = 0; gg < ng; ++gg) w += part[gg * nb + r];
+        const double tw = ti * w;
+        for (int c = c0; c < c1; ++c) M[r + c * ldm] = fma(-tw, (c == i) ? 1.0 : S[i + c * lds], M[r + c * ldm]);
+      }
+      __syncthreads();
+    }
+    // ---- LQ of M (dgelq2): row i, columns i..nb2-1 ----
+    for (int i = 0; i < nb; ++i) {
+      double ps = 0.0;
+      for (int c = i + 1 + t; c < nb2; c += nt) ps = fma(M[i + c * ldm], M[i + c * ldm], ps);
+      const double ss = block_sum(ps, red);
+      const Reflector h = make_reflector(M[i + i * ldm], ss);
+      __syncthreads();
+      for (int c = i + 1 + t; c < nb2; c += nt) M[i + c * ldm] *= h.scal;
+      __syncthreads();
+      if (h.tau != 0.0 && i + 1 < nb) {
+        const int ng = nt / nb;
+        const int r = t % nb, g = t / nb;
+        const int len = nb2 - i;
+        const int cpart = (len + ng - 1) / ng;
+        const int c0 = i + g * cpart, c1 = min(nb2, c0 + cpart);
+        double s = 0.0;
+        if (r > i)
+          for (int c = c0; c < c1; ++c) s = fma(M[r + c * ldm], (c == i) ? 1.0 : M[i + c * ldm], s);
+        part[g * nb + r] = s;
+        __syncthreads();
+        if (r > i) {
+          double w = 0.0;
+          for (int gg = 0; gg < ng; ++gg) w += part[gg * nb + r];
+          const double tw = h.tau * w;
+          for (int c = c0; c < c1; ++c) M[r + c * ldm] = fma(-tw, (c == i) ? 1.0 : M[i + c * ldm], M[r + c * ldm]);
+        }
+      }
+      __syncthreads();
+      if (t == 0) {
+        M[i + i * ldm] = h.beta;
+        tauL[i] = h.tau;
+      }
+      __syncthreads();
+    }
+    // VRc[c][i] = VR[i][c]: unit at c == i, M[i][c] for c > i, zero before.
+    for (int e = t; e < L * nb; e += nt) {
+      const int c = e % L, i = e / L;
+      double v = 0.0;
+      if (c < nb2) v = (c < i) ? 0.0 : (c == i ? 1.0 : M[i + c * ldm]);
+      V[c + (size_t)i * L] = v;
+    }
+    // G[q][m] = VR[q] . VR[m] for q < m
+    for (int e = t; e < nb * nb; e += nt) {
+      const int q = e % nb, m = e / nb;
+      double s = 0.0;
+      if (q < m) {
+        s = M[q + m * ldm];
+        for (int c = m + 1; c < nb2; ++c) s = fma(M[q + c * ldm], M[m + c * ldm], s);
+      }
+      G[q + m * nb] = s;
+    }
+    __syncthreads();
+    form_t_forward(nb, G, nb, tauL, Ts, nb, Tout, nb);
+  } else {
+    // Backward row-wise reflectors straight from the RQ (ab2rht.f90:308-309).
+    const int k = nb2;
+    for (int e = t; e < L * nb; e += nt) {
+      const int c = e % L, i = e / L;
+      double v = 0.0;
+      if (i < k && c < nb2) v = (c < i) ? S[i + c * lds] : (c == i ? 1.0 : 0.0);
+      V[c + (size_t)i * L] = v;
+    }
+    // G[l][i] = v_l . v_i for l > i (support of v_i: columns 0..i)
+    for (int e = t; e < nb * nb; e += nt) {
+      const int l = e % nb, i = e / nb;
+      double s = 0.0;
+      if (l > i && l < k) {
+        s = S[l + i * lds];  // v_l[i] * v_i[i](=1)
+        for (int c = 0; c < i; ++c) s = fma(S[l + c * lds], S[i + c * lds], s);
+      }
+      G[l + i * nb] = s;
+    }
+    __syncthreads();
+    form_t_backward(k, G, nb, tauR, Ts, nb, Tout, nb);
+  }
+}
+
+// Zero B(j+1 : ib2, j) for the first nb columns of the block (ab2rht.f90:329-333).
+__global__ void k_s1_zero_fill(double* B, int ldb, int ib0, int ib2, int nb) {
+  const int j = ib0 + blockIdx.x;
+  for (int i = j + 1 + threadIdx.x; i <= ib2; i += blockDim.x) B[(size_t)i + (size_t)j * ldb] = 0.0;
+}
+
+// ------------------------------------------------------------------------------------------
+// Host driver
+// ------------------------------------------------------------------------------------------
+
+size_t s1_workspace_bytes(int n, int nb, int p) {
+  const int L = p * nb;
+  const int nblk0 = std::max(1, (n - nb + (p - 1) * nb - 1) / ((p - 1) * nb));
+  size_t w = 0;
+  w += (size_t)L * nb * nblk0 * 2;   // VL, VRc
+  w += (size_t)nb * nb * nblk0 * 2;  // TL, TR
+  w += (size_t)(L + 1) * L + (size_t)nb * (L + 1);  // global scratch for big right-gen tiles
+  return w * sizeof(double) + 4096;
+}
+
+static size_t left_gen_smem(int L, int nb) { return sizeof(double) * ((size_t)(L + 1) * nb + 2 * nb * nb + nb + 32); }
+static size_t right_gen_small(int L, int nb) {
+  return sizeof(double) * ((size_t)L + nb + 2 * (size_t)nb * nb + 32 + kRgenThreads);
+}
+static size_t right_gen_big(int L, int nb) { return sizeof(double) * ((size_t)(L + 1) * L + (size_t)nb * (L + 1)); }
+
+int s1_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, int ldq, double* Z, int ldz, int nb, int p,
+           PhaseTimer* timer) {
+  if (n - nb - 1 < 1) return 0;  // ab2rht.f90:71: empty panel loop
+  const int L = p * nb;
+  cudaStream_t s = ctx.stream;
+  const int nblk0 = std::max(1, (n - nb + (p - 1) * nb - 1) / ((p - 1) * nb));
+  double* ws = (double*)ctx.workspace(s1_workspace_bytes(n, nb, p));
+  if (!ws) return PARAHT_ERR_ALLOC;
+  double* VL = ws;
+  double* VRc = VL + (size_t)L * nb * nblk0;
+  double* TL = VRc + (size_t)L * nb * nblk0;
+  double* TR = TL + (size_t)nb * nb * nblk0;
+  double* gscr = TR + (size_t)nb * nb * nblk0;
+
+  const size_t lsm = left_gen_smem(L, nb);
+  const size_t rsm_small = right_gen_small(L, nb);
+  const bool r_in_smem = rsm_small + right_gen_big(L, nb) <= (size_t)ctx.max_smem;
+  const size_t rsm = r_in_smem ? rsm_small + right_gen_big(L, nb) : rsm_small;
+  if (lsm > (size_t)ctx.max_smem || rsm_small > (size_t)ctx.max_smem) return PARAHT_ERR_NOT_SUPPORTED;
+  cudaFuncSetAttribute(k_s1_left_gen, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsm);
+  cudaFuncSetAttribute(k_s1_right_gen, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm);
+
+  for (int jb0 = 0; jb0 <= n - nb - 2; jb0 += nb) {  // ab2rht.f90:71 (1-based jb = 1 .. n-nb-1)
+    const S1Panel P = make_panel(n, nb, p, jb0);
+    if (timer) timer->mark(s, 0);
+    k_s1_left_gen<<<1, kGenThreads, lsm, s>>>(A, lda, P, VL, TL);
+    if (timer) timer->mark(s, 2);
+    launch_apply_left(B, ldb, P.ib(P.nblocks - 1), n - 1, GeoS1Left{P, VL, TL, 0}, s);
+    launch_apply_left(A, lda, jb0 + nb, n - 1, GeoS1Left{P, VL, TL, 1}, s);
+    launch_apply_right(Q, ldq, 0, n - 1, GeoS1Q{P, VL, TL}, s);
+    if (timer) timer->mark(s, 1);
+    for (int o = 0; o < P.nblocks; ++o) {
+      k_s1_right_gen<<<1, kRgenThreads, rsm, s>>>(B, ldb, P, o, VRc, TR, r_in_smem ? nullptr : gscr);
+      launch_apply_right(B, ldb, 0, P.ib2(o), GeoS1Right{P, VRc, TR, o}, s);
+      if (P.nb2(o) > nb) k_s1_zero_fill<<<nb, 128, 0, s>>>(B, ldb, P.ib(o), P.ib2(o), nb);
+    }
+    if (timer) timer->mark(s, 2);
+    launch_apply_right(A, lda, 0, n - 1, GeoS1Right{P, VRc, TR, -1}, s);
+    launch_apply_right(Z, ldz, 0, n - 1, GeoS1Right{P, VRc, TR, -1}, s);
+  }
+  if (timer) timer->mark(s, -1);
+  return 0;
+}
+
+}  // namespace pht

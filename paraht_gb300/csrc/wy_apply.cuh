@@ -1,0 +1,219 @@
+// wy_apply.cuh -- FP64 application of ordered compact-WY op lists to column strips / row strips.
+//
+// Each CTA owns a strip of the target matrix (CS columns for left ops, RS rows for right ops)
+// and walks the whole op list in order, applying every op that touches the strip.  Ops that
+// overlap are therefore applied in list order for every entry, which is the ordering the
+// reference's taskloops give each row/column chunk (e.g. src/ab2rht.f90:149-166,
+// src/rht2ht.f90:1818-1844).  Strips are independent, so there is no inter-CTA sync.
+//
+// Geometry classes provide   int count() const;   pht::WYOp op(int i) const;   (device)
+#pragma once
+#include "paraht_internal.cuh"
+
+namespace pht {
+
+constexpr int kApplyThreads = 256;
+constexpr int kLeftCS = 32;    // columns per CTA (left ops)
+constexpr int kLeftRCH = 128;  // row chunk staged in shared memory
+constexpr int kRightRS = 64;   // rows per CTA (right ops)
+constexpr int kRightCCH = 64;  // column chunk staged in shared memory
+constexpr int kMaxK = 64;      // max reflectors per op
+
+// X <- H^T X on columns [col0 + blockIdx.x*CS, ...] for every op (dlarfb 'L','T','F','C').
+template <class Geo>
+__global__ void __launch_bounds__(kApplyThreads) k_apply_left(double* __restrict__ X, int ldx, int col0, int col1,
+                                                               Geo g) {
+  extern __shared__ double smx[];
+  double(*Xs)[kLeftCS + 1] = reinterpret_cast<double(*)[kLeftCS + 1]>(smx);
+  double(*W)[kLeftCS + 1] = reinterpret_cast<double(*)[kLeftCS + 1]>(smx + kLeftRCH * (kLeftCS + 1));
+  const int t = threadIdx.x;
+  const int cbeg = col0 + blockIdx.x * kLeftCS;
+  if (cbeg > col1) return;
+  const int cend = min(col1, cbeg + kLeftCS - 1);
+  const int nops = g.count();
+  for (int o = 0; o < nops; ++o) {
+    const WYOp op = g.op(o);
+    const int ca = max(cbeg, op.lo), cb = min(cend, op.hi);
+    if (ca > cb || op.k <= 0 || op.len <= 0) continue;
+    const int w = cb - ca + 1;
+    const int k = op.k;
+    // ---- pass 1: W = V^T X_sub (k x w) ----
+    for (int i = t; i < kMaxK * kLeftCS; i += kApplyThreads) W[i / kLeftCS][i % kLeftCS] = 0.0;
+    for (int r0 = 0; r0 < op.len; r0 += kLeftRCH) {
+      const int rl = min(kLeftRCH, op.len - r0);
+      __syncthreads();
+      for (int e = t; e < kLeftRCH * kLeftCS; e += kApplyThreads) {
+        const int i = e % kLeftRCH, c = e / kLeftRCH;
+        Xs[i][c] = (i < rl && c < w) ? X[(size_t)(op.start + r0 + i) + (size_t)(ca + c) * ldx] : 0.0;
+      }
+      __syncthreads();
+      const int c = t % kLeftCS, mg = t / kLeftCS;  // 8 groups of m
+      for (int m = mg; m < k; m += kApplyThreads / kLeftCS) {
+        const double* v = op.V + (size_t)m * op.ldv + r0;
+        double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+        int i = 0;
+        for (; i + 3 < rl; i += 4) {
+          a0 = fma(v[i], Xs[i][c], a0);
+          a1 = fma(v[i + 1], Xs[i + 1][c], a1);
+          a2 = fma(v[i + 2], Xs[i + 2][c], a2);
+          a3 = fma(v[i + 3], Xs[i + 3][c], a3);
+        }
+        for (; i < rl; ++i) a0 = fma(v[i], Xs[i][c], a0);
+        W[m][c] += (a0 + a1) + (a2 + a3);
+      }
+    }
+    __syncthreads();
+    // ---- W2 = T^T W: W2[m] = sum_l T[l][m] W[l]  (T is stored with explicit zeros) ----
+    {
+      const int c = t % kLeftCS, mg = t / kLeftCS;
+      double acc[kMaxK / (kApplyThreads / kLeftCS)];
+      int cnt = 0;
+      for (int m = mg; m < k; m += kApplyThreads / kLeftCS) {
+        const double* tc = op.T + (size_t)m * op.ldt;
+        double s = 0.0;
+        for (int l = 0; l < k; ++l) s = fma(tc[l], W[l][c], s);
+        acc[cnt++] = s;
+      }
+      __syncthreads();
+      cnt = 0;
+      for (int m = mg; m < k; m += kApplyThreads / kLeftCS) W[m][c] = acc[cnt++];
+    }
+    // ---- pass 2: X_sub -= V W2 ----
+    for (int r0 = 0; r0 < op.len; r0 += kLeftRCH) {
+      const int rl = min(kLeftRCH, op.len - r0);
+      __syncthreads();
+      for (int e = t; e < kLeftRCH * kLeftCS; e += kApplyThreads) {
+        const int i = e % kLeftRCH, c = e / kLeftRCH;
+        if (i < rl && c < w) Xs[i][c] = X[(size_t)(op.start + r0 + i) + (size_t)(ca + c) * ldx];
+      }
+      __syncthreads();
+      const int c = t % kLeftCS;
+      for (int i = t / kLeftCS; i < rl; i += kApplyThreads / kLeftCS) {
+        double s = 0.0;
+        for (int m = 0; m < k; ++m) s = fma(op.V[(size_t)m * op.ldv + r0 + i], W[m][c], s);
+        Xs[i][c] -= s;
+      }
+      __syncthreads();
+      for (int e = t; e < kLeftRCH * kLeftCS; e += kApplyThreads) {
+        const int i = e % kLeftRCH, c = e / kLeftRCH;
+        if (i < rl && c < w) X[(size_t)(op.start + r0 + i) + (size_t)(ca + c) * ldx] = Xs[i][c];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// X <- X H on rows [row0 + blockIdx.x*RS, ...] for every op (dlarfb 'R','N','F','C').
+template <class Geo>
+__global__ void __launch_bounds__(kApplyThreads) k_apply_right(double* __restrict__ X, int ldx, int row0, int row1,
+                                                                Geo g) {
+  extern __shared__ double smx[];
+  double(*Xs)[kRightRS + 1] = reinterpret_cast<double(*)[kRightRS + 1]>(smx);
+  double(*Y)[kRightRS + 1] = reinterpret_cast<double(*)[kRightRS + 1]>(smx + kRightCCH * (kRightRS + 1));
+  const int t = threadIdx.x;
+  const int rbeg = row0 + blockIdx.x * kRightRS;
+  if (rbeg > row1) return;
+  const int rend = min(row1, rbeg + kRightRS - 1);
+  const int nops = g.count();
+  constexpr int kGroups = kApplyThreads / kRightRS;  // 4
+  for (int o = 0; o < nops; ++o) {
+    const WYOp op = g.op(o);
+    const int ra = max(rbeg, op.lo), rb = min(rend, op.hi);
+    if (ra > rb || op.k <= 0 || op.len <= 0) continue;
+    const int h = rb - ra + 1;
+    const int k = op.k;
+    for (int i = t; i < kMaxK * kRightRS; i += kApplyThreads) Y[i / kRightRS][i % kRightRS] = 0.0;
+    // ---- pass 1: Y = X_sub V (h x k) ----
+    for (int c0 = 0; c0 < op.len; c0 += kRightCCH) {
+      const int cl = min(kRightCCH, op.len - c0);
+      __syncthreads();
+      for (int e = t; e < kRightCCH * kRightRS; e += kApplyThreads) {
+        const int rr = e % kRightRS, c = e / kRightRS;
+        Xs[c][rr] = (rr < h && c < cl) ? X[(size_t)(ra + rr) + (size_t)(op.start + c0 + c) * ldx] : 0.0;
+      }
+      __syncthreads();
+      const int rr = t % kRightRS, mg = t / kRightRS;
+      for (int m = mg; m < k; m += kGroups) {
+        const double* v = op.V + (size_t)m * op.ldv + c0;
+        double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+        int c = 0;
+        for (; c + 3 < cl; c += 4) {
+          a0 = fma(Xs[c][rr], v[c], a0);
+          a1 = fma(Xs[c + 1][rr], v[c + 1], a1);
+          a2 = fma(Xs[c + 2][rr], v[c + 2], a2);
+          a3 = fma(Xs[c + 3][rr], v[c + 3], a3);
+        }
+        for (; c < cl; ++c) a0 = fma(Xs[c][rr], v[c], a0);
+        Y[m][rr] += (a0 + a1) + (a2 + a3);
+      }
+    }
+    __syncthreads();
+    // ---- Y2 = Y T: Y2[m] = sum_l Y[l] T[l][m]  (upper T for forward, lower for backward) ----
+    {
+      const int rr = t % kRightRS, mg = t / kRightRS;
+      double acc[kMaxK / kGroups];
+      int cnt = 0;
+      for (int m = mg; m < k; m += kGroups) {
+        const double* tc = op.T + (size_t)m * op.ldt;
+        double s = 0.0;
+        for (int l = 0; l < k; ++l) s = fma(Y[l][rr], tc[l], s);
+        acc[cnt++] = s;
+      }
+      __syncthreads();
+      cnt = 0;
+      for (int m = mg; m < k; m += kGroups) Y[m][rr] = acc[cnt++];
+    }
+    // ---- pass 2: X_sub -= Y2 V^T ----
+    for (int c0 = 0; c0 < op.len; c0 += kRightCCH) {
+      const int cl = min(kRightCCH, op.len - c0);
+      __syncthreads();
+      for (int e = t; e < kRightCCH * kRightRS; e += kApplyThreads) {
+        const int rr = e % kRightRS, c = e / kRightRS;
+        if (rr < h && c < cl) Xs[c][rr] = X[(size_t)(ra + rr) + (size_t)(op.start + c0 + c) * ldx];
+      }
+      __syncthreads();
+      const int rr = t % kRightRS;
+      for (int c = t / kRightRS; c < cl; c += kGroups) {
+        double s = 0.0;
+        for (int m = 0; m < k; ++m) s = fma(Y[m][rr], op.V[(size_t)m * op.ldv + c0 + c], s);
+        Xs[c][rr] -= s;
+      }
+      __syncthreads();
+      for (int e = t; e < kRightCCH * kRightRS; e += kApplyThreads) {
+        const int rr = e % kRightRS, c = e / kRightRS;
+        if (rr < h && c < cl) X[(size_t)(ra + rr) + (size_t)(op.start + c0 + c) * ldx] = Xs[c][rr];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+constexpr size_t kLeftSmem = sizeof(double) * (size_t)(kLeftRCH + kMaxK) * (kLeftCS + 1);
+constexpr size_t kRightSmem = sizeof(double) * (size_t)(kRightCCH + kMaxK) * (kRightRS + 1);
+
+// Launch helpers: one CTA per strip; the dynamic shared-memory opt-in is set once per
+// instantiation.
+template <class Geo>
+inline void launch_apply_left(double* X, int ldx, int col0, int col1, const Geo& g, cudaStream_t s) {
+  if (col1 < col0) return;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_apply_left<Geo>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLeftSmem);
+    attr = true;
+  }
+  const int nblk = (col1 - col0 + 1 + kLeftCS - 1) / kLeftCS;
+  k_apply_left<Geo><<<nblk, kApplyThreads, kLeftSmem, s>>>(X, ldx, col0, col1, g);
+}
+template <class Geo>
+inline void launch_apply_right(double* X, int ldx, int row0, int row1, const Geo& g, cudaStream_t s) {
+  if (row1 < row0) return;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_apply_right<Geo>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRightSmem);
+    attr = true;
+  }
+  const int nblk = (row1 - row0 + 1 + kRightRS - 1) / kRightRS;
+  k_apply_right<Geo><<<nblk, kApplyThreads, kRightSmem, s>>>(X, ldx, row0, row1, g);
+}
+
+}  // namespace pht

@@ -1,0 +1,88 @@
+"""CPU tests of the C ABI boundary: the library loads, exports every declared symbol, and
+validates arguments (LAPACK INFO-style negative indices) before touching the GPU."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from paraht_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "paraht.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\*?\s+\*?(paraht_\w+)\s*\(", src, flags=re.M)))
+
+
+def test_library_loads_and_exports_every_declared_symbol():
+    L = _lib.lib()
+    names = declared_symbols()
+    assert len(names) >= 15
+    for name in names:
+        assert hasattr(L, name), name
+    assert set(names) == set(_lib.SIGNATURES), set(names) ^ set(_lib.SIGNATURES)
+    assert L.paraht_version() == 100
+    assert L.paraht_strerror(-1002) == b"allocation failed"
+
+
+def _args(n=10, lda=None, r=4, p=2, nq=2):
+    A = np.zeros((max(n, 1), max(n, 1)), order="F")
+    lda = lda if lda is not None else max(n, 1)
+    ptr = A.ctypes.data
+    return A, [n, ptr, lda, ptr, lda, ptr, lda, ptr, lda, r, p, nq, 0]
+
+
+@pytest.mark.parametrize("field,value,expected", [
+    (0, -1, -1),    # n
+    (2, 0, -3),     # lda < n
+    (4, 3, -5),     # ldb
+    (6, 3, -7),     # ldq
+    (8, 3, -9),     # ldz
+    (9, 0, -10),    # r < 1
+    (9, 65, -10),   # r > 64
+    (10, 1, -11),   # p < 2
+    (11, 0, -12),   # nq < 1
+    (11, 5, -12),   # nq > r (outside the reference's valid domain)
+])
+def test_reduce_argument_errors(field, value, expected):
+    A, args = _args()
+    args[field] = value
+    assert _lib.lib().paraht_reduce(*args) == expected
+
+
+def test_null_pointer_and_stage_entry_errors():
+    L = _lib.lib()
+    A, args = _args()
+    args[1] = None
+    assert L.paraht_reduce(*args) == -2
+    A, args = _args()
+    # ab2rht: (n, A, lda, B, ldb, Q, ldq, Z, ldz, nb, p, time_components)
+    assert L.paraht_ab2rht(*(args[:9] + [4, 1, 0])) == -11
+    # rht2ht: (..., r, nq, time_components)
+    assert L.paraht_rht2ht(*(args[:9] + [4, 9, 0])) == -11
+    assert L.paraht_reduce(*([0] + args[1:])) == 0  # n = 0: quick return
+
+
+def test_context_entry_points_reject_bad_context():
+    L = _lib.lib()
+    A, args = _args()
+    assert L.paraht_reduce_d(None, *args) == -1007
+    assert L.paraht_ctx_destroy(None) == -1007
+    buf = (C.c_double * 8)()
+    assert L.paraht_ctx_phase_times(None, buf, 8) == -1007
+
+
+def test_python_wrapper_raises_with_argument_index():
+    import paraht_gb300 as ph
+
+    n = 8
+    A = np.zeros((n, n), order="F")
+    with pytest.raises(ph.ParahtError) as e:
+        ph.ab2rht_simple(n, A, n, A, n, A, n, A, n, 4, 1, False)
+    assert e.value.status == -11
+    with pytest.raises(TypeError):
+        ph.ab2rht_simple(n, np.zeros((n, n)), n, A, n, A, n, A, n, 4, 2, False)  # C order rejected

@@ -1,0 +1,136 @@
+"""GPU parity tests: the CUDA path (through the C ABI) against the CPU oracle.
+
+Tolerances (FP64 path):
+* stage-level outputs (same input fed to both): elementwise relative difference <= 1e-9, since
+  both follow the same sequence of Householder transformations and differ only by rounding;
+* final pencil: backward errors and orthogonality <= 10*n*eps (the acceptance bound), |H|, |T|
+  elementwise within 1e-8 of the oracle's (essential uniqueness: Q e1 = e1 on both sides);
+* structure: exact zeros below the Hessenberg / triangular structure.
+"""
+import numpy as np
+import pytest
+
+import paraht_gb300 as ph
+from helpers import EPS, abs_rel_max_diff, bwd, copies, eig_mismatch, make, oracle_reduce, orth, rel_max_diff
+from paraht_gb300.generate import identity
+
+pytestmark = pytest.mark.gpu
+
+STAGE_CASES = [
+    # n, r, p, nq
+    (5, 2, 2, 2),
+    (17, 3, 3, 2),
+    (33, 4, 2, 3),
+    (64, 8, 4, 4),
+    (100, 16, 8, 8),
+    (130, 8, 2, 8),
+    (257, 16, 8, 8),
+    (300, 16, 4, 16),
+    (333, 32, 4, 8),
+]
+
+
+@pytest.mark.parametrize("n,r,p,nq", STAGE_CASES)
+def test_stage1_matches_oracle(oracle, n, r, p, nq):
+    A0, B0 = make(n)
+    Ao, Bo, Qo, Zo = oracle_reduce(oracle, A0, B0, r, p, nq, stage=1)
+    A, B = copies(A0, B0)
+    Q, Z = identity(n), identity(n)
+    ph.ab2rht_simple(n, A, n, B, n, Q, n, Z, n, r, p, False)
+    assert np.all(np.tril(A, -r - 1) == 0.0)
+    assert np.all(np.tril(B, -1) == 0.0)
+    # the oracle keeps roundoff below the structure; the GPU path zeroes it
+    for X, Xo in ((A, np.triu(Ao, -r)), (B, np.triu(Bo)), (Q, Qo), (Z, Zo)):
+        assert rel_max_diff(X, Xo) < 1e-9
+    assert bwd(Q, A0, Z, A) <= 10 * n * EPS
+    assert bwd(Q, B0, Z, B) <= 10 * n * EPS
+
+
+@pytest.mark.parametrize("n,r,p,nq", STAGE_CASES)
+def test_stage2_matches_oracle(oracle, n, r, p, nq):
+    A0, B0 = make(n)
+    A1, B1, Q1, Z1 = oracle_reduce(oracle, A0, B0, r, p, nq, stage=1)
+    Ao, Bo, Qo, Zo = copies(A1, B1, Q1, Z1)
+    oracle.rht2ht_householder(Ao, Bo, Qo, Zo, r, nq)
+    A, B, Q, Z = copies(A1, B1, Q1, Z1)
+    ph.rht2ht_householder(n, A, n, B, n, Q, n, Z, n, r, nq, False)
+    assert np.all(np.tril(A, -2) == 0.0)
+    assert np.all(np.tril(B, -1) == 0.0)
+    assert rel_max_diff(A, np.triu(Ao, -1)) < 1e-9
+    assert rel_max_diff(B, np.triu(Bo)) < 1e-9
+    assert rel_max_diff(Q, Qo) < 1e-9
+    assert rel_max_diff(Z, Zo) < 1e-9
+
+
+@pytest.mark.parametrize("n,r,p,nq,dist", [
+    (200, 16, 8, 8, "std"),
+    (256, 8, 2, 4, "std_qr"),
+    (180, 16, 4, 16, "graded"),
+    (150, 4, 8, 3, "refcompat"),
+])
+def test_reduce_end_to_end(oracle, ctx, n, r, p, nq, dist):
+    A0, B0 = make(n, dist)
+    A, B = copies(A0, B0)
+    Q, Z = identity(n), identity(n)
+    ctx.reduce_host(A, B, Q, Z, r, p, nq, flags=ph.PARAHT_FLAG_TIME_COMPONENTS)
+    tol = 10 * n * EPS
+    assert bwd(Q, A0, Z, A) <= tol
+    assert bwd(Q, B0, Z, B) <= tol
+    assert orth(Q) <= tol and orth(Z) <= tol
+    assert np.all(np.tril(A, -2) == 0.0) and np.all(np.tril(B, -1) == 0.0)
+    Ao, Bo, Qo, Zo = oracle_reduce(oracle, A0, B0, r, p, nq)
+    if dist != "graded":  # graded has a singular T: the HT form is no longer essentially unique
+        assert abs_rel_max_diff(A, Ao) < 1e-8
+        assert abs_rel_max_diff(B, Bo) < 1e-8
+    t = ctx.phase_times()
+    assert t["total"] > 0 and t["s1_genleft"] > 0 and t["s2_gen"] > 0
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 6, 9])
+def test_tiny_sizes(oracle, n):
+    r, p, nq = 2, 2, 2
+    A0, B0 = make(n)
+    A, B = copies(A0, B0)
+    Q, Z = identity(n), identity(n)
+    ph.reduce(A, B, Q, Z, r, p, nq)
+    Ao, Bo, Qo, Zo = oracle_reduce(oracle, A0, B0, r, p, nq)
+    assert rel_max_diff(np.abs(A), np.abs(np.triu(Ao, -1))) < 1e-10
+    assert rel_max_diff(np.abs(B), np.abs(np.triu(Bo))) < 1e-10
+    assert bwd(Q, A0, Z, A) <= 10 * max(n, 2) * EPS
+
+
+def test_eigenvalues_match(oracle, ctx):
+    n, r, p, nq = 120, 8, 4, 8
+    A0, B0 = make(n)
+    A, B = copies(A0, B0)
+    Q, Z = identity(n), identity(n)
+    ctx.reduce_host(A, B, Q, Z, r, p, nq)
+    Ao, Bo, _, _ = oracle_reduce(oracle, A0, B0, r, p, nq)
+    ar, ai, be, info = oracle.dhgeqz_eigs(A, B)
+    aro, aio, beo, info2 = oracle.dhgeqz_eigs(Ao, Bo)
+    assert info == 0 and info2 == 0
+    assert eig_mismatch((ar + 1j * ai) / be, (aro + 1j * aio) / beo) < 1e-8
+
+
+def test_nonfinite_input_rejected(ctx):
+    n = 20
+    A0, B0 = make(n)
+    A, B = copies(A0, B0)
+    A[3, 4] = np.nan
+    with pytest.raises(ph.ParahtError) as e:
+        ctx.reduce_host(A, B, identity(n), identity(n), 4, 2, 2, flags=ph.PARAHT_FLAG_CHECK_FINITE)
+    assert e.value.status == -1004
+
+
+def test_device_pointer_entry_matches_host(ctx):
+    torch = pytest.importorskip("torch")
+    n, r, p, nq = 160, 8, 4, 8
+    A0, B0 = make(n)
+    A, B = copies(A0, B0)
+    Q, Z = identity(n), identity(n)
+    ctx.reduce_host(A, B, Q, Z, r, p, nq)
+    dev = [torch.from_numpy(np.ascontiguousarray(X.T)).cuda() for X in (A0, B0, identity(n), identity(n))]
+    ctx.reduce_d(n, dev[0].data_ptr(), n, dev[1].data_ptr(), n, dev[2].data_ptr(), n, dev[3].data_ptr(), n, r, p, nq)
+    torch.cuda.synchronize()
+    for X, D in zip((A, B, Q, Z), dev):
+        assert np.array_equal(X, D.cpu().numpy().T)
