@@ -1,0 +1,329 @@
+#!/usr/bin/env python3
+"""Headline benchmark: seconds for the two-stage HT reduction of one n=16000 pencil on one GB300.
+
+Metric (BASELINE): "HT-reduction sec at n=16000: split-prec vs FP64 GPU at bwd err<=1e-13".
+A step is one full reduction (stage 1 + stage 2, Q and Z accumulated) of the synthetic pencil
+"std" (A ~ N(0,1), B the R factor of a Gaussian matrix, seed 1302) with the reference's
+parameter surface (r, p, nq).  Arrays are column-major FP64 resident in HBM; the pristine input
+is restored (device-to-device copy) before every step, outside the timed region.  The inputs
+(4 x n^2 x 8 B = 8.2 GB at n=16000) are far larger than L2, so no extra L2 flush is needed.
+
+* ``value``: mean device time per step (CUDA events on the library's stream, max over ranks).
+* ``e2e``:   the same reduction through the public host entry point paraht_reduce_host with
+             pinned host buffers, host<->device copies inside the timed region.
+* ``cpu_baseline``: the CPU oracle (a restatement of the reference's OpenMP algorithm) on a
+             bounded sample, scaled by (n / n_sample)^3 to the metric's unit.
+* ``--impl reference``: times that CPU implementation on the host cores (the reference itself
+             is Fortran and cannot be compiled on this image).
+
+Multi-GPU: the single-pencil path does not shard (replicas only): with N ranks every rank
+reduces its own pencil; value = max-over-ranks step time / N (job seconds per reduction).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "HT-reduction sec at n=16000: split-prec vs FP64 GPU at bwd err<=1e-13"
+EPS = float(np.finfo(np.float64).eps)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("paraht", "reference"), default="paraht")
+    ap.add_argument("--n", type=int, default=16000)
+    ap.add_argument("--r", type=int, default=16)
+    ap.add_argument("--p", type=int, default=2)
+    ap.add_argument("--nq", type=int, default=16)
+    ap.add_argument("--dist", default="std")
+    ap.add_argument("--precision", choices=("fp64", "split"), default="fp64")
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--cpu-sample-n", type=int, default=2500)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--check", action="store_true", help="also compute the backward error of the last step")
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def _run(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                f = [x.strip() for x in out.stdout.strip().split(",")]
+                if len(f) >= 7:
+                    self.samples.append(f)
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def flops_nominal(n: int) -> float:
+    # fixed nominal count used for "effective GFLOP/s" (stage 1 at p=8 plus stage 2): 18.67 n^3
+    return 18.67 * float(n) ** 3
+
+
+def cpu_oracle_seconds(n_sample: int, r: int, p: int, nq: int, dist: str):
+    """Times the CPU oracle (restatement of the reference's OpenMP ParaHT) once on n_sample."""
+    from oracle import oracle as O
+    from paraht_gb300.generate import identity, pencil
+
+    O.set_blas_threads(1)
+    A, B = pencil(n_sample, dist, seed=1302)
+    Q, Z = identity(n_sample), identity(n_sample)
+    t0 = time.perf_counter()
+    O.reduce(A, B, Q, Z, min(r, n_sample), p, min(nq, r))
+    return time.perf_counter() - t0
+
+
+def run_reference(args, rank: int):
+    """--impl reference: the CPU implementation of the path on the host cores."""
+    if rank != 0:
+        return 0
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    ns = args.cpu_sample_n
+    for _ in range(args.warmup):
+        cpu_oracle_seconds(max(200, ns // 4), args.r, args.p, args.nq, args.dist)
+    ts = [cpu_oracle_seconds(ns, args.r, args.p, args.nq, args.dist) for _ in range(max(1, args.steps))]
+    scale = (args.n / ns) ** 3
+    v = statistics.mean(ts) * scale
+    line = {
+        "metric": METRIC, "value": v, "unit": "s", "impl": "reference", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": statistics.mean(ts) * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"HT reduction n={args.n} r={args.r} p={args.p} nq={args.nq} dist={args.dist}",
+                   "n": args.n, "r": args.r, "p": args.p, "nq": args.nq},
+        "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port",
+                         "sample": f"oracle (C/OpenMP restatement of ab2rht_simple+rht2ht_householder, single-threaded "
+                                   f"BLAS inside tasks) at n={ns}, mean of {len(ts)} runs, scaled by (n/{ns})^3"},
+        "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank)
+
+    import torch
+
+    import paraht_gb300 as ph
+    from paraht_gb300.generate import pencil
+
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
+    torch.cuda.set_device(local)
+    dist_on = world > 1
+    if dist_on:
+        import torch.distributed as td
+
+        td.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist_on:
+            import torch.distributed as td
+
+            td.barrier()
+
+    n, r, p, nq = args.n, args.r, args.p, args.nq
+    flags = ph.PARAHT_FLAG_SPLIT if args.precision == "split" else 0
+    A0, B0 = pencil(n, args.dist, seed=1302 + rank)
+    # pristine inputs on the device (column-major: a row-major tensor of the transpose)
+    dev0 = [torch.from_numpy(np.ascontiguousarray(X.T)).cuda() for X in (A0, B0)]
+    eye = torch.eye(n, dtype=torch.float64, device="cuda")
+    work = [torch.empty_like(eye) for _ in range(4)]
+    ctx = ph.Context(local)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+
+    def restore():
+        with torch.cuda.stream(stream):
+            work[0].copy_(dev0[0])
+            work[1].copy_(dev0[1])
+            work[2].copy_(eye)
+            work[3].copy_(eye)
+        stream.synchronize()
+
+    def step(f=flags):
+        ctx.reduce_d(n, work[0].data_ptr(), n, work[1].data_ptr(), n, work[2].data_ptr(), n, work[3].data_ptr(), n,
+                     r, p, nq, f)
+
+    for _ in range(args.warmup):
+        restore()
+        step()
+    torch.cuda.synchronize()
+    ms = []
+    launches = 0
+    sampler = ClockSampler(local)
+    with sampler:
+        for _ in range(args.steps):
+            restore()
+            barrier()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+            launches += ctx.launch_count()
+            barrier()
+    t_step = statistics.mean(ms) / 1e3
+    if dist_on:
+        import torch.distributed as td
+
+        tt = torch.tensor([t_step], device="cuda")
+        td.all_reduce(tt, op=td.ReduceOp.MAX)
+        t_step = float(tt.item())
+    value = t_step / world
+
+    # backward error of the last timed step (outside the timed region)
+    check = None
+    if args.check:
+        Qd, Zd = work[2], work[3]
+        A0d = dev0[0]
+        # column-major data stored as row-major transposes: X^T tensors -> use .T views
+        H, T, Q, Z = work[0].T, work[1].T, Qd.T, Zd.T
+        Af, Bf = A0d.T, dev0[1].T
+        ea = float(torch.linalg.norm(Q.T @ Af @ Z - H) / torch.linalg.norm(Af))
+        eb = float(torch.linalg.norm(Q.T @ Bf @ Z - T) / torch.linalg.norm(Bf))
+        check = {"bwd_err_A": ea, "bwd_err_B": eb, "bound_10n_eps": 10 * n * EPS}
+
+    # one instrumented step for the phase breakdown (time_components serialises the streams)
+    restore()
+    step(flags | ph.PARAHT_FLAG_TIME_COMPONENTS)
+    phases = ctx.phase_times()
+
+    # end to end through the public host entry point (pinned host buffers, copies timed)
+    hostA = torch.from_numpy(np.asfortranarray(A0).T.copy()).pin_memory()
+    hostB = torch.from_numpy(np.asfortranarray(B0).T.copy()).pin_memory()
+    hostQ = torch.empty((n, n), dtype=torch.float64).pin_memory()
+    hostZ = torch.empty((n, n), dtype=torch.float64).pin_memory()
+    e2e_t = []
+    for i in range(args.e2e_steps + 1):
+        hostA.copy_(torch.from_numpy(np.asfortranarray(A0).T))
+        hostB.copy_(torch.from_numpy(np.asfortranarray(B0).T))
+        hostQ.copy_(torch.eye(n, dtype=torch.float64))
+        hostZ.copy_(torch.eye(n, dtype=torch.float64))
+        nA, nB, nQ, nZ = (x.numpy().T for x in (hostA, hostB, hostQ, hostZ))  # Fortran-ordered views
+        barrier()
+        t0 = time.perf_counter()
+        ctx.reduce_host(nA, nB, nQ, nZ, r, p, nq, flags)
+        dt = time.perf_counter() - t0
+        if i > 0 or args.e2e_steps == 0:  # first call sizes the staging buffers
+            e2e_t.append(dt)
+    e2e_v = statistics.mean(e2e_t) / world
+
+    # roofline of the dominant phase (stage-1 and stage-2 bulk updates run on FP64 CUDA cores)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    f1 = 4.0 * p / (p - 1) * (7.0 / 3.0) * n ** 3  # stage-1 useful flops
+    f2 = 8.0 * n ** 3                                 # stage-2 useful flops
+    t1 = phases["s1_genleft"] + phases["s1_genright"] + phases["s1_mul"]
+    t2 = phases["s2_gen"] + phases["s2_lookahead"] + phases["s2_application"]
+    fp64_peak = 1.19  # TFLOP/s, FP64 FMA throughput measured on this GB300 (not in MEASURED_PEAKS.json)
+    mul_t = phases["s1_mul"] + phases["s2_application"]
+    mul_f = f1 + f2
+    achieved = mul_f / mul_t / 1e12 if mul_t > 0 else None
+    roofline = {
+        "bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+        "frac": (achieved / fp64_peak) if achieved else None, "traffic": None,
+        "kernel": "k_apply_left/k_apply_right (compact-WY bulk updates, FP64 CUDA cores)",
+        "peak_source": "FP64 FMA throughput measured on this pool's GB300 (1.19 TFLOP/s); MEASURED_PEAKS.json "
+                       f"lists HBM {peaks.get('hbm_gbs')} GB/s and bf16 {peaks.get('bf16_tflops')} TFLOP/s only",
+        "stage_seconds": {"stage1": t1, "stage2": t2},
+    }
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        ns = args.cpu_sample_n
+        ts = cpu_oracle_seconds(ns, r, p, nq, args.dist)
+        cpu = {"value": ts * (n / ns) ** 3, "unit": "s", "cores": int(os.environ.get("OMP_NUM_THREADS",
+                                                                                        os.cpu_count() or 1)),
+               "kind": "port",
+               "sample": f"CPU oracle (OpenMP restatement of the reference) at n={ns}: {ts:.2f} s, scaled by (n/{ns})^3"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"HT reduction of one pencil n={n} (A N(0,1), B triangular Gaussian R), "
+                                   f"r={r} p={p} nq={nq}, {args.precision}",
+                       "n": n, "r": r, "p": p, "nq": nq, "precision": args.precision, "dist": args.dist,
+                       "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "inputs 8.2 GB >> L2; pristine input restored between steps outside the timed region"},
+            "e2e": {"value": e2e_v, "unit": "s", "h2d_bytes_per_step": 4 * n * n * 8, "d2h_bytes_per_step": 4 * n * n * 8},
+            "gpu_launches": launches,
+            "phases_s": {k: round(v, 4) for k, v in phases.items()},
+            "effective_gflops": flops_nominal(n) / t_step / 1e9,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": sampler.summary(),
+        }
+        if check:
+            line["check"] = check
+        print(json.dumps(line), flush=True)
+    if dist_on:
+        import torch.distributed as td
+
+        td.destroy_process_group()
+    ctx.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -50,6 +50,9 @@ extern "C" {
 #define PARAHT_FLAG_CHECK_FINITE 2    /* reject non-finite inputs before reducing */
 #define PARAHT_FLAG_SPLIT 4           /* split-precision (emulated FP64) bulk updates */
 #define PARAHT_FLAG_NO_ZERO_FILL 8    /* keep roundoff below the structure instead of exact zeros */
+#define PARAHT_FLAG_SEQUENTIAL 16     /* debug: run the stage-2 sweeps of a group one after the other in
+                                         one CTA and all updates on one stream (the reference's order);
+                                         results are bitwise identical to the default pipelined schedule */
 
 typedef struct paraht_ctx_s* paraht_ctx;
 
@@ -64,6 +67,8 @@ int paraht_ctx_set_stream(paraht_ctx ctx, void* stream);
  *   [6] host<->device copies (host entry points only)             [7] total device time
  * (the groups printed by src/ab2rht.f90:487-490 and src/rht2ht.f90:2044-2047). */
 int paraht_ctx_phase_times(paraht_ctx ctx, double* times, int ntimes);
+/* Number of GPU kernels the library launched during the last call on this context. */
+int paraht_ctx_launch_count(paraht_ctx ctx, long long* count);
 /* Largest absolute entry found below the structure (r-Hessenberg / Hessenberg for A,
  * triangular for B) before it was zeroed by the last call: [0] A, [1] B. */
 int paraht_ctx_fill_residue(paraht_ctx ctx, double* residue, int nres);

@@ -22,12 +22,13 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import (PARAHT_FLAG_CHECK_FINITE, PARAHT_FLAG_NO_ZERO_FILL, PARAHT_FLAG_SPLIT,
+from ._lib import (PARAHT_FLAG_CHECK_FINITE, PARAHT_FLAG_NO_ZERO_FILL, PARAHT_FLAG_SEQUENTIAL, PARAHT_FLAG_SPLIT,
                    PARAHT_FLAG_TIME_COMPONENTS, ParahtError, check, lib)
 
 __all__ = [
     "ab2rht_simple", "rht2ht_householder", "reduce", "Context", "ParahtError",
     "PARAHT_FLAG_TIME_COMPONENTS", "PARAHT_FLAG_CHECK_FINITE", "PARAHT_FLAG_SPLIT", "PARAHT_FLAG_NO_ZERO_FILL",
+    "PARAHT_FLAG_SEQUENTIAL",
 ]
 
 PHASE_NAMES = ("s1_genleft", "s1_genright", "s1_mul", "s2_gen", "s2_lookahead", "s2_application", "copies", "total")
@@ -120,6 +121,11 @@ class Context:
         buf = (C.c_double * 8)()
         check(lib().paraht_ctx_phase_times(self._h, buf, 8), "phase_times")
         return dict(zip(PHASE_NAMES, list(buf)))
+
+    def launch_count(self) -> int:
+        v = C.c_longlong()
+        check(lib().paraht_ctx_launch_count(self._h, C.byref(v)), "launch_count")
+        return int(v.value)
 
     def fill_residue(self):
         buf = (C.c_double * 2)()

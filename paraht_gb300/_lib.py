@@ -14,6 +14,7 @@ PARAHT_FLAG_TIME_COMPONENTS = 1
 PARAHT_FLAG_CHECK_FINITE = 2
 PARAHT_FLAG_SPLIT = 4
 PARAHT_FLAG_NO_ZERO_FILL = 8
+PARAHT_FLAG_SEQUENTIAL = 16
 
 ERRORS = {
     -1001: "PARAHT_ERR_CUDA",
@@ -34,6 +35,7 @@ SIGNATURES = {
     "paraht_ctx_set_stream": [C.c_void_p, C.c_void_p],
     "paraht_ctx_phase_times": [C.c_void_p, C.POINTER(C.c_double), _i],
     "paraht_ctx_fill_residue": [C.c_void_p, C.POINTER(C.c_double), _i],
+    "paraht_ctx_launch_count": [C.c_void_p, C.POINTER(C.c_longlong)],
     "paraht_ab2rht": [_i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i, _i],
     "paraht_rht2ht": [_i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i, _i],
     "paraht_reduce": [_i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i, _i, _i],

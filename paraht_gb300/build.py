@@ -19,6 +19,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libparaht.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"] + ARCH
+# Per-file flags: the pipelined chase reads data other CTAs wrote, so its global loads bypass L1.
+FILE_FLAGS = {"stage2_chase.cu": ["-Xptxas", "-dlcm=cg"]}
 
 
 def nvcc() -> str:
@@ -64,7 +66,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
-        cmd = [nvcc(), "-c", src, "-o", obj] + flags
+        cmd = [nvcc(), "-c", src, "-o", obj] + flags + FILE_FLAGS.get(os.path.basename(src), [])
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

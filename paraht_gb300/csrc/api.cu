@@ -6,8 +6,13 @@
 #include <algorithm>
 #include <new>
 
+#include "launch_count.h"
 #include "paraht_impl.h"
 #include "paraht_internal.cuh"
+
+namespace pht {
+thread_local long long tl_launches = 0;
+}
 
 struct paraht_ctx_s {
   pht::Ctx c;
@@ -75,6 +80,7 @@ __global__ void k_zero_fill(int n, double* X, int ldx, int band, unsigned long l
 void zero_fill(cudaStream_t s, int n, double* A, int lda, int band, double* B, int ldb, double* dres) {
   if (n <= 1) return;
   cudaMemsetAsync(dres, 0, 2 * sizeof(double), s);
+  count_launch(2);
   k_zero_fill<<<n, 128, 0, s>>>(n, A, lda, band, (unsigned long long*)dres);
   k_zero_fill<<<n, 128, 0, s>>>(n, B, ldb, 0, (unsigned long long*)(dres + 1));
 }
@@ -87,6 +93,7 @@ __global__ void k_check_finite(int n, const double* X, int ldx, int* flag) {
 
 int check_finite(cudaStream_t s, int n, const double* A, int lda, const double* B, int ldb, int* dflag) {
   cudaMemsetAsync(dflag, 0, sizeof(int), s);
+  count_launch(2);
   k_check_finite<<<n, 256, 0, s>>>(n, A, lda, dflag);
   k_check_finite<<<n, 256, 0, s>>>(n, B, ldb, dflag);
   int h = 0;
@@ -123,6 +130,9 @@ extern "C" int paraht_ctx_create(paraht_ctx* out, int device) {
   int rc = 0;
   if (cudaStreamCreateWithFlags(&x.stream, cudaStreamNonBlocking) != cudaSuccess) rc = PARAHT_ERR_CUDA;
   x.own_stream = true;
+  if (!rc && cudaStreamCreateWithFlags(&x.side, cudaStreamNonBlocking) != cudaSuccess) rc = PARAHT_ERR_CUDA;
+  if (!rc && cudaEventCreateWithFlags(&x.ev_a, cudaEventDisableTiming) != cudaSuccess) rc = PARAHT_ERR_CUDA;
+  if (!rc && cudaEventCreateWithFlags(&x.ev_b, cudaEventDisableTiming) != cudaSuccess) rc = PARAHT_ERR_CUDA;
   if (!rc && cudaMalloc(&x.dstatus, 64) != cudaSuccess) rc = PARAHT_ERR_ALLOC;
   if (!rc && cudaMalloc(&x.dresidue, 2 * sizeof(double)) != cudaSuccess) rc = PARAHT_ERR_ALLOC;
   cudaSetDevice(prev);
@@ -148,6 +158,12 @@ extern "C" int paraht_ctx_destroy(paraht_ctx c) {
   if (x.dstatus) cudaFree(x.dstatus);
   if (x.dresidue) cudaFree(x.dresidue);
   if (x.own_stream && x.stream) cudaStreamDestroy(x.stream);
+  if (x.side) {
+    cudaStreamSynchronize(x.side);
+    cudaStreamDestroy(x.side);
+  }
+  if (x.ev_a) cudaEventDestroy(x.ev_a);
+  if (x.ev_b) cudaEventDestroy(x.ev_b);
   cudaSetDevice(prev);
   c->magic = 0;
   delete c;
@@ -176,6 +192,13 @@ extern "C" int paraht_ctx_phase_times(paraht_ctx c, double* t, int nt) {
   if (!t && nt > 0) return -2;
   for (int i = 0; i < nt && i < 8; ++i) t[i] = c->c.phase[i];
   for (int i = 8; i < nt; ++i) t[i] = 0.0;
+  return 0;
+}
+
+extern "C" int paraht_ctx_launch_count(paraht_ctx c, long long* count) {
+  if (!ctx_ok(c)) return PARAHT_ERR_BAD_CTX;
+  if (!count) return -2;
+  *count = c->c.launches;
   return 0;
 }
 
@@ -222,13 +245,16 @@ static int finish(Ctx& x) {
 // Runs the selected stages on device-resident arrays (stream-ordered; caller synchronises).
 static int run_device(Ctx& x, int which, int n, double* A, int lda, double* B, int ldb, double* Q, int ldq, double* Z,
                       int ldz, int r, int p, int nq, int flags) {
+  x.launches = 0;
   if (n == 0) return 0;
   if (flags & PARAHT_FLAG_SPLIT) return PARAHT_ERR_NOT_SUPPORTED;
+  const long long launches0 = pht::tl_launches;
   const bool timed = flags & PARAHT_FLAG_TIME_COMPONENTS;
   if (flags & PARAHT_FLAG_CHECK_FINITE) {
     const int rc = pht::check_finite(x.stream, n, A, lda, B, ldb, x.dstatus);
     if (rc) return rc;
   }
+  cudaMemsetAsync(x.dstatus, 0, sizeof(int), x.stream);
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (timed) {
     cudaEventCreate(&e0);
@@ -236,6 +262,7 @@ static int run_device(Ctx& x, int which, int n, double* A, int lda, double* B, i
     cudaEventRecord(e0, x.stream);
   }
   int rc = 0;
+  x.sequential_chase = (flags & PARAHT_FLAG_SEQUENTIAL) ? 1 : 0;
   if (which & 1) {
     x.timer.reset(0);
     rc = pht::s1_run(x, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, p, timed ? &x.timer : nullptr);
@@ -252,6 +279,8 @@ static int run_device(Ctx& x, int which, int n, double* A, int lda, double* B, i
       x.timer.accumulate(x.phase, 8);
     }
   }
+  int hstatus = 0;
+  if (!rc) cudaMemcpyAsync(&hstatus, x.dstatus, sizeof(int), cudaMemcpyDeviceToHost, x.stream);
   if (!rc && !(flags & PARAHT_FLAG_NO_ZERO_FILL)) {
     pht::zero_fill(x.stream, n, A, lda, (which & 2) ? 1 : r, B, ldb, x.dresidue);
     cudaMemcpyAsync(x.residue, x.dresidue, 2 * sizeof(double), cudaMemcpyDeviceToHost, x.stream);
@@ -264,6 +293,9 @@ static int run_device(Ctx& x, int which, int n, double* A, int lda, double* B, i
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
   }
+  if (!rc) rc = finish(x);
+  if (!rc && hstatus) rc = hstatus;
+  x.launches = pht::tl_launches - launches0;
   return rc;
 }
 

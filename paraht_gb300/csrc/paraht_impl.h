@@ -54,10 +54,15 @@ struct Ctx {
   size_t ws_bytes = 0;
   double* stage[4] = {nullptr, nullptr, nullptr, nullptr};  // device copies for host entries
   size_t stage_bytes = 0;
+  cudaStream_t side = nullptr;      // second stream for work that overlaps the critical path
+  cudaEvent_t ev_a = nullptr, ev_b = nullptr;
+  int sequential_chase = 0;         // 1: run stage-2 sweeps one after the other in one CTA
+  long long spin_limit = 1ll << 24;  // polls before a device-side wait gives up
   int* dstatus = nullptr;  // device status word
   PhaseTimer timer;
   double phase[8] = {0};
   double residue[2] = {0};
+  long long launches = 0;  // kernels launched by the last call
   double* dresidue = nullptr;
   void* workspace(size_t bytes);
   int ensure_staging(size_t bytes_each);

@@ -466,6 +466,7 @@ int s1_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
   for (int jb0 = 0; jb0 <= n - nb - 2; jb0 += nb) {  // ab2rht.f90:71 (1-based jb = 1 .. n-nb-1)
     const S1Panel P = make_panel(n, nb, p, jb0);
     if (timer) timer->mark(s, 0);
+    count_launch();
     k_s1_left_gen<<<1, kGenThreads, lsm, s>>>(A, lda, P, VL, TL);
     if (timer) timer->mark(s, 2);
     launch_apply_left(B, ldb, P.ib(P.nblocks - 1), n - 1, GeoS1Left{P, VL, TL, 0}, s);
@@ -473,6 +474,7 @@ int s1_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
     launch_apply_right(Q, ldq, 0, n - 1, GeoS1Q{P, VL, TL}, s);
     if (timer) timer->mark(s, 1);
     for (int o = 0; o < P.nblocks; ++o) {
+      count_launch(1 + (P.nb2(o) > nb));
       k_s1_right_gen<<<1, kRgenThreads, rsm, s>>>(B, ldb, P, o, VRc, TR, r_in_smem ? nullptr : gscr);
       launch_apply_right(B, ldb, 0, P.ib2(o), GeoS1Right{P, VRc, TR, o}, s);
       if (P.nb2(o) > nb) k_s1_zero_fill<<<nb, 128, 0, s>>>(B, ldb, P.ib(o), P.ib2(o), nb);

@@ -8,6 +8,7 @@
 //
 // Geometry classes provide   int count() const;   pht::WYOp op(int i) const;   (device)
 #pragma once
+#include "launch_count.h"
 #include "paraht_internal.cuh"
 
 namespace pht {
@@ -202,6 +203,7 @@ inline void launch_apply_left(double* X, int ldx, int col0, int col1, const Geo&
     attr = true;
   }
   const int nblk = (col1 - col0 + 1 + kLeftCS - 1) / kLeftCS;
+  count_launch();
   k_apply_left<Geo><<<nblk, kApplyThreads, kLeftSmem, s>>>(X, ldx, col0, col1, g);
 }
 template <class Geo>
@@ -213,6 +215,7 @@ inline void launch_apply_right(double* X, int ldx, int row0, int row1, const Geo
     attr = true;
   }
   const int nblk = (row1 - row0 + 1 + kRightRS - 1) / kRightRS;
+  count_launch();
   k_apply_right<Geo><<<nblk, kApplyThreads, kRightSmem, s>>>(X, ldx, row0, row1, g);
 }
 

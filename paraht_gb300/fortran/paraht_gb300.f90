@@ -1,0 +1,93 @@
+! paraht_gb300.f90 -- Fortran drop-in for the reduction path, calling libparaht (include/paraht.h)
+! through ISO_C_BINDING.
+!
+! The modules `ab2rht` and `rht2ht` export `ab2rht_simple` and `rht2ht_householder` with exactly
+! the argument lists of the reference (src/ab2rht.f90:8-13, src/rht2ht.f90:1346-1351), so a
+! caller such as src/profilereduction.f90 only needs to be recompiled against this file and
+! linked with -lparaht.  Arrays stay on the host; each call copies them to the GPU, reduces and
+! copies them back.  An optional trailing INFO argument returns the library status (0 = ok,
+! -i = i-th argument invalid, <= -1000 = PARAHT_ERR_*); without it a failure is reported on
+! standard error (the reference itself performs no error reporting).
+!
+! Build (not done by this repository: the image has no Fortran compiler):
+!   gfortran -O2 -c paraht_gb300.f90
+!   gfortran ... your_program.f90 paraht_gb300.o -L<dir of libparaht.so> -lparaht -Wl,-rpath,<dir>
+
+module paraht_c
+   use iso_c_binding, only: c_int, c_double
+   implicit none
+   interface
+      integer(c_int) function paraht_ab2rht(n, A, lda, B, ldb, Q, ldq, Z, ldz, nb, p, time_components) &
+         bind(C, name="paraht_ab2rht")
+         import :: c_int, c_double
+         integer(c_int), value :: n, lda, ldb, ldq, ldz, nb, p, time_components
+         real(c_double) :: A(*), B(*), Q(*), Z(*)
+      end function paraht_ab2rht
+
+      integer(c_int) function paraht_rht2ht(n, A, lda, B, ldb, Q, ldq, Z, ldz, r, nq, time_components) &
+         bind(C, name="paraht_rht2ht")
+         import :: c_int, c_double
+         integer(c_int), value :: n, lda, ldb, ldq, ldz, r, nq, time_components
+         real(c_double) :: A(*), B(*), Q(*), Z(*)
+      end function paraht_rht2ht
+
+      integer(c_int) function paraht_reduce(n, A, lda, B, ldb, Q, ldq, Z, ldz, r, p, nq, flags) &
+         bind(C, name="paraht_reduce")
+         import :: c_int, c_double
+         integer(c_int), value :: n, lda, ldb, ldq, ldz, r, p, nq, flags
+         real(c_double) :: A(*), B(*), Q(*), Z(*)
+      end function paraht_reduce
+   end interface
+
+contains
+
+   subroutine paraht_report(who, status, info)
+      character(len=*), intent(in) :: who
+      integer(c_int), intent(in) :: status
+      integer, intent(out), optional :: info
+      if (present(info)) then
+         info = int(status)
+      else if (status /= 0) then
+         write(0, '(A,A,I0)') who, ': libparaht status ', status
+      end if
+   end subroutine paraht_report
+
+end module paraht_c
+
+module ab2rht
+   use paraht_c
+   implicit none
+contains
+   ! src/ab2rht.f90:8 -- stage 1, (A, B) -> (r-Hessenberg, upper triangular); Q <- Q*Q1, Z <- Z*Z1
+   subroutine ab2rht_simple(n, A, lda, B, ldb, Q, ldq, Z, ldz, nb, p, time_components, info)
+      integer, intent(in) :: n, lda, ldb, ldq, ldz, nb, p
+      double precision, intent(inout) :: A(lda,*), B(ldb,*), Z(ldz,*), Q(ldq,*)
+      logical :: time_components
+      integer, intent(out), optional :: info
+      integer(c_int) :: status, tc
+      tc = 0
+      if (time_components) tc = 1
+      status = paraht_ab2rht(int(n, c_int), A, int(lda, c_int), B, int(ldb, c_int), Q, int(ldq, c_int), &
+         Z, int(ldz, c_int), int(nb, c_int), int(p, c_int), tc)
+      call paraht_report('ab2rht_simple', status, info)
+   end subroutine ab2rht_simple
+end module ab2rht
+
+module rht2ht
+   use paraht_c
+   implicit none
+contains
+   ! src/rht2ht.f90:1346 -- stage 2, r-Hessenberg -> Hessenberg; Q, Z accumulated
+   subroutine rht2ht_householder(n, A, lda, B, ldb, Q, ldq, Z, ldz, r, nq, time_components, info)
+      integer, intent(in) :: n, lda, ldb, ldq, ldz, r, nq
+      double precision, intent(inout) :: A(lda,*), B(ldb,*), Z(ldz,*), Q(ldq,*)
+      logical :: time_components
+      integer, intent(out), optional :: info
+      integer(c_int) :: status, tc
+      tc = 0
+      if (time_components) tc = 1
+      status = paraht_rht2ht(int(n, c_int), A, int(lda, c_int), B, int(ldb, c_int), Q, int(ldq, c_int), &
+         Z, int(ldz, c_int), int(r, c_int), int(nq, c_int), tc)
+      call paraht_report('rht2ht_householder', status, info)
+   end subroutine rht2ht_householder
+end module rht2ht
