@@ -133,6 +133,9 @@ extern "C" int paraht_ctx_create(paraht_ctx* out, int device) {
   if (!rc && cudaStreamCreateWithFlags(&x.side, cudaStreamNonBlocking) != cudaSuccess) rc = PARAHT_ERR_CUDA;
   if (!rc && cudaEventCreateWithFlags(&x.ev_a, cudaEventDisableTiming) != cudaSuccess) rc = PARAHT_ERR_CUDA;
   if (!rc && cudaEventCreateWithFlags(&x.ev_b, cudaEventDisableTiming) != cudaSuccess) rc = PARAHT_ERR_CUDA;
+  if (!rc && cudaStreamCreateWithFlags(&x.side2, cudaStreamNonBlocking) != cudaSuccess) rc = PARAHT_ERR_CUDA;
+  for (auto& e : x.ev)
+    if (!rc && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) rc = PARAHT_ERR_CUDA;
   if (!rc && cudaMalloc(&x.dstatus, 64) != cudaSuccess) rc = PARAHT_ERR_ALLOC;
   if (!rc && cudaMalloc(&x.dresidue, 2 * sizeof(double)) != cudaSuccess) rc = PARAHT_ERR_ALLOC;
   cudaSetDevice(prev);
@@ -162,8 +165,14 @@ extern "C" int paraht_ctx_destroy(paraht_ctx c) {
     cudaStreamSynchronize(x.side);
     cudaStreamDestroy(x.side);
   }
+  if (x.side2) {
+    cudaStreamSynchronize(x.side2);
+    cudaStreamDestroy(x.side2);
+  }
   if (x.ev_a) cudaEventDestroy(x.ev_a);
   if (x.ev_b) cudaEventDestroy(x.ev_b);
+  for (auto e : x.ev)
+    if (e) cudaEventDestroy(e);
   cudaSetDevice(prev);
   c->magic = 0;
   delete c;

@@ -55,7 +55,9 @@ struct Ctx {
   double* stage[4] = {nullptr, nullptr, nullptr, nullptr};  // device copies for host entries
   size_t stage_bytes = 0;
   cudaStream_t side = nullptr;      // second stream for work that overlaps the critical path
+  cudaStream_t side2 = nullptr;     // third stream (bulk updates that feed nothing on the critical path)
   cudaEvent_t ev_a = nullptr, ev_b = nullptr;
+  cudaEvent_t ev[8] = {};           // stage-1 dependency events
   int sequential_chase = 0;         // 1: run stage-2 sweeps one after the other in one CTA
   long long spin_limit = 1ll << 24;  // polls before a device-side wait gives up
   int* dstatus = nullptr;  // device status word

@@ -17,101 +17,10 @@
 
 #include "paraht_internal.cuh"
 #include "paraht_impl.h"
+#include "stage1_geom.cuh"
 #include "wy_apply.cuh"
 
 namespace pht {
-
-// ------------------------------------------------------------------------------------------
-// Panel geometry (0-based).  Block o (o = 0 .. nblocks-1) is the o-th block from the bottom.
-// ------------------------------------------------------------------------------------------
-struct S1Panel {
-  int n, nb, p, jb0;  // jb0: first panel column (0-based)
-  int nblocks, ibtop0, stride, L;
-  PHT_DEV __host__ int ib(int o) const { return ibtop0 - o * stride; }
-  PHT_DEV __host__ int ib2(int o) const { return min(n - 1, ib(o) + L - 1); }
-  PHT_DEV __host__ int nb2(int o) const { return ib2(o) - ib(o) + 1; }
-};
-
-static S1Panel make_panel(int n, int nb, int p, int jb0) {
-  S1Panel g;
-  g.n = n;
-  g.nb = nb;
-  g.p = p;
-  g.jb0 = jb0;
-  const int m = n - nb - jb0;  // rows jb0+nb .. n-1  (ab2rht.f90:74: n-nb-jb+1 with 1-based jb)
-  g.stride = (p - 1) * nb;
-  g.nblocks = (m + g.stride - 1) / g.stride;
-  g.L = p * nb;
-  g.ibtop0 = jb0 + nb + (g.nblocks - 1) * g.stride;
-  return g;
-}
-
-// Left ops of the panel on B (columns >= ib) or A (columns >= jb+nb): dlarfb('L','T','F','C').
-struct GeoS1Left {
-  S1Panel P;
-  const double* VL;
-  const double* TL;
-  int onA;
-  PHT_DEV int count() const { return P.nblocks; }
-  PHT_DEV WYOp op(int o) const {
-    WYOp w;
-    w.start = P.ib(o);
-    w.len = P.nb2(o);
-    w.k = min(P.nb, w.len);
-    w.lo = onA ? P.jb0 + P.nb : P.ib(o);
-    w.hi = P.n - 1;
-    w.V = VL + (size_t)o * P.L * P.nb;
-    w.ldv = P.L;
-    w.T = TL + (size_t)o * P.nb * P.nb;
-    w.ldt = P.nb;
-    return w;
-  }
-};
-
-// Right ops of the panel's left reflectors on Q: Q(:, ib:ib2) <- Q H (ab2rht.f90:241).
-struct GeoS1Q {
-  S1Panel P;
-  const double* VL;
-  const double* TL;
-  PHT_DEV int count() const { return P.nblocks; }
-  PHT_DEV WYOp op(int o) const {
-    WYOp w;
-    w.start = P.ib(o);
-    w.len = P.nb2(o);
-    w.k = min(P.nb, w.len);
-    w.lo = 0;
-    w.hi = P.n - 1;
-    w.V = VL + (size_t)o * P.L * P.nb;
-    w.ldv = P.L;
-    w.T = TL + (size_t)o * P.nb * P.nb;
-    w.ldt = P.nb;
-    return w;
-  }
-};
-
-// Right reflectors (stored transposed in VRc) on A, Z (all rows) or on B (rows up to ib2 of a
-// single block, bl_only >= 0).
-struct GeoS1Right {
-  S1Panel P;
-  const double* VRc;
-  const double* TR;
-  int bl_only;  // -1: all blocks, all rows; else only block bl_only, rows [0, ib2]
-  PHT_DEV int count() const { return bl_only >= 0 ? 1 : P.nblocks; }
-  PHT_DEV WYOp op(int i) const {
-    const int o = bl_only >= 0 ? bl_only : i;
-    WYOp w;
-    w.start = P.ib(o);
-    w.len = P.nb2(o);
-    w.k = (w.len > P.nb) ? P.nb : w.len;
-    w.lo = 0;
-    w.hi = bl_only >= 0 ? P.ib2(o) : P.n - 1;
-    w.V = VRc + (size_t)o * P.L * P.nb;
-    w.ldv = P.L;
-    w.T = TR + (size_t)o * P.nb * P.nb;
-    w.ldt = P.nb;
-    return w;
-  }
-};
 
 // ------------------------------------------------------------------------------------------
 // Triangular factor of a block reflector from the Gram matrix of its vectors:
@@ -425,13 +334,14 @@ __global__ void k_s1_zero_fill(double* B, int ldb, int ib0, int ib2, int nb) {
 // Host driver
 // ------------------------------------------------------------------------------------------
 
+static int s1_nblk0(int n, int nb, int p) { return std::max(1, (n - nb + (p - 1) * nb - 1) / ((p - 1) * nb)); }
+
 size_t s1_workspace_bytes(int n, int nb, int p) {
   const int L = p * nb;
-  const int nblk0 = std::max(1, (n - nb + (p - 1) * nb - 1) / ((p - 1) * nb));
+  const size_t nblk0 = s1_nblk0(n, nb, p);
   size_t w = 0;
-  w += (size_t)L * nb * nblk0 * 2;   // VL, VRc
-  w += (size_t)nb * nb * nblk0 * 2;  // TL, TR
-  w += (size_t)(L + 1) * L + (size_t)nb * (L + 1);  // global scratch for big right-gen tiles
+  w += 2 * ((size_t)L * nb * nblk0 * 2 + (size_t)nb * nb * nblk0 * 2);  // two sets of VL, VRc, TL, TR
+  w += (size_t)(L + 1) * L + (size_t)nb * (L + 1);                      // global scratch (large-L fallback)
   return w * sizeof(double) + 4096;
 }
 
@@ -441,49 +351,139 @@ static size_t right_gen_small(int L, int nb) {
 }
 static size_t right_gen_big(int L, int nb) { return sizeof(double) * ((size_t)(L + 1) * L + (size_t)nb * (L + 1)); }
 
+size_t s1_lgen_smem(int L, int nb);
+size_t s1_rgen_smem(int L, int nb);
+void launch_s1_lgen(cudaStream_t s, double* A, int lda, const S1Panel& P, double* VL, double* TL);
+void launch_s1_rgen(cudaStream_t s, const double* B, int ldb, const S1Panel& P, int o, double* VRc, double* TR);
+
+// Stage-1 schedule.  Three streams, as the reference's task graph (ab2rht.f90:85-467) allows:
+//   sA (critical): left generation, left update of B, then per block the right generation and
+//       the update of the B rows the next block needs (the reference's "lookahead",
+//       rows ib-(p-1)nb .. ib2, ab2rht.f90:317-338), then the right update of A;
+//   sB: per block, the update of the remaining B rows 1 .. ib-(p-1)nb-1 (ab2rht.f90:343-367),
+//       which the lookahead of the next block waits for (the B(3,3) token);
+//   sC: left updates of A and Q and the right update of Z (priority-1 tasks).
+// Reflector sets alternate between two buffers so that panel k+1 can be generated while sC
+// still applies panel k.  With time_components everything runs on sA (the reference inserts
+// taskwaits for the same purpose).
 int s1_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, int ldq, double* Z, int ldz, int nb, int p,
            PhaseTimer* timer) {
   if (n - nb - 1 < 1) return 0;  // ab2rht.f90:71: empty panel loop
   const int L = p * nb;
-  cudaStream_t s = ctx.stream;
-  const int nblk0 = std::max(1, (n - nb + (p - 1) * nb - 1) / ((p - 1) * nb));
+  const bool serial = timer != nullptr;
+  cudaStream_t sA = ctx.stream, sB = serial ? sA : ctx.side, sC = serial ? sA : ctx.side2;
+  const size_t nblk0 = s1_nblk0(n, nb, p);
   double* ws = (double*)ctx.workspace(s1_workspace_bytes(n, nb, p));
   if (!ws) return PARAHT_ERR_ALLOC;
-  double* VL = ws;
-  double* VRc = VL + (size_t)L * nb * nblk0;
-  double* TL = VRc + (size_t)L * nb * nblk0;
-  double* TR = TL + (size_t)nb * nb * nblk0;
-  double* gscr = TR + (size_t)nb * nb * nblk0;
+  double *VL[2], *VRc[2], *TL[2], *TR[2];
+  double* d = ws;
+  for (int k = 0; k < 2; ++k) {
+    VL[k] = d;
+    VRc[k] = VL[k] + (size_t)L * nb * nblk0;
+    TL[k] = VRc[k] + (size_t)L * nb * nblk0;
+    TR[k] = TL[k] + (size_t)nb * nb * nblk0;
+    d = TR[k] + (size_t)nb * nb * nblk0;
+  }
+  double* gscr = d;
 
+  // fast latency-oriented generation kernels (stage1_gen.cu) when the tiles fit; else the
+  // general kernels above
+  const bool fast_l = nb <= 64 && s1_lgen_smem(L, nb) <= (size_t)ctx.max_smem;
+  const bool fast_r = L <= 128 && s1_rgen_smem(L, nb) <= (size_t)ctx.max_smem;
   const size_t lsm = left_gen_smem(L, nb);
   const size_t rsm_small = right_gen_small(L, nb);
   const bool r_in_smem = rsm_small + right_gen_big(L, nb) <= (size_t)ctx.max_smem;
   const size_t rsm = r_in_smem ? rsm_small + right_gen_big(L, nb) : rsm_small;
-  if (lsm > (size_t)ctx.max_smem || rsm_small > (size_t)ctx.max_smem) return PARAHT_ERR_NOT_SUPPORTED;
-  cudaFuncSetAttribute(k_s1_left_gen, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsm);
-  cudaFuncSetAttribute(k_s1_right_gen, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm);
+  if ((!fast_l && lsm > (size_t)ctx.max_smem) || (!fast_r && rsm_small > (size_t)ctx.max_smem))
+    return PARAHT_ERR_NOT_SUPPORTED;
+  if (!fast_l) cudaFuncSetAttribute(k_s1_left_gen, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsm);
+  if (!fast_r) cudaFuncSetAttribute(k_s1_right_gen, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm);
 
-  for (int jb0 = 0; jb0 <= n - nb - 2; jb0 += nb) {  // ab2rht.f90:71 (1-based jb = 1 .. n-nb-1)
-    const S1Panel P = make_panel(n, nb, p, jb0);
-    if (timer) timer->mark(s, 0);
-    count_launch();
-    k_s1_left_gen<<<1, kGenThreads, lsm, s>>>(A, lda, P, VL, TL);
-    if (timer) timer->mark(s, 2);
-    launch_apply_left(B, ldb, P.ib(P.nblocks - 1), n - 1, GeoS1Left{P, VL, TL, 0}, s);
-    launch_apply_left(A, lda, jb0 + nb, n - 1, GeoS1Left{P, VL, TL, 1}, s);
-    launch_apply_right(Q, ldq, 0, n - 1, GeoS1Q{P, VL, TL}, s);
-    if (timer) timer->mark(s, 1);
-    for (int o = 0; o < P.nblocks; ++o) {
-      count_launch(1 + (P.nb2(o) > nb));
-      k_s1_right_gen<<<1, kRgenThreads, rsm, s>>>(B, ldb, P, o, VRc, TR, r_in_smem ? nullptr : gscr);
-      launch_apply_right(B, ldb, 0, P.ib2(o), GeoS1Right{P, VRc, TR, o}, s);
-      if (P.nb2(o) > nb) k_s1_zero_fill<<<nb, 128, 0, s>>>(B, ldb, P.ib(o), P.ib2(o), nb);
-    }
-    if (timer) timer->mark(s, 2);
-    launch_apply_right(A, lda, 0, n - 1, GeoS1Right{P, VRc, TR, -1}, s);
-    launch_apply_right(Z, ldz, 0, n - 1, GeoS1Right{P, VRc, TR, -1}, s);
+  cudaEvent_t evL = ctx.ev[0], evAL = ctx.ev[1], evLA = ctx.ev[2], evRest = ctx.ev[3], evChain = ctx.ev[4];
+  cudaEvent_t evZ[2] = {ctx.ev[5], ctx.ev[6]};
+  if (!serial) {  // side streams start after everything already queued on sA
+    cudaEventRecord(evL, sA);
+    cudaStreamWaitEvent(sB, evL, 0);
+    cudaStreamWaitEvent(sC, evL, 0);
+    cudaEventRecord(evRest, sB);
+    cudaEventRecord(evZ[0], sC);
+    cudaEventRecord(evZ[1], sC);
   }
-  if (timer) timer->mark(s, -1);
+  int k = 0;
+  for (int jb0 = 0; jb0 <= n - nb - 2; jb0 += nb, ++k) {  // ab2rht.f90:71 (1-based jb = 1 .. n-nb-1)
+    const S1Panel P = make_panel(n, nb, p, jb0);
+    const int s = k & 1;
+    if (timer) timer->mark(sA, 0);
+    if (!serial) cudaStreamWaitEvent(sA, evZ[s], 0);  // set s free again (Z update of panel k-2 done)
+    if (fast_l) {
+      launch_s1_lgen(sA, A, lda, P, VL[s], TL[s]);
+    } else {
+      count_launch();
+      k_s1_left_gen<<<1, kGenThreads, lsm, sA>>>(A, lda, P, VL[s], TL[s]);
+    }
+    if (timer) timer->mark(sA, 2);
+    if (!serial) {
+      cudaEventRecord(evL, sA);
+      cudaStreamWaitEvent(sC, evL, 0);
+      cudaStreamWaitEvent(sA, evRest, 0);  // remaining-row B updates of panel k-1 done
+    }
+    launch_apply_left(B, ldb, P.ib(P.nblocks - 1), n - 1, GeoS1Left{P, VL[s], TL[s], 0}, sA);
+    launch_apply_left(A, lda, jb0 + nb, n - 1, GeoS1Left{P, VL[s], TL[s], 1}, sC);
+    if (!serial) cudaEventRecord(evAL, sC);
+    launch_apply_right(Q, ldq, 0, n - 1, GeoS1Q{P, VL[s], TL[s]}, sC);
+    if (timer) timer->mark(sA, 1);
+    if (!serial) {
+      cudaEventRecord(evLA, sA);  // B left update done: the remaining-row updates may start
+      cudaStreamWaitEvent(sB, evLA, 0);
+    }
+    for (int o = 0; o < P.nblocks; ++o) {
+      if (fast_r) {
+        launch_s1_rgen(sA, B, ldb, P, o, VRc[s], TR[s]);
+      } else {
+        count_launch();
+        k_s1_right_gen<<<1, kRgenThreads, rsm, sA>>>(B, ldb, P, o, VRc[s], TR[s], r_in_smem ? nullptr : gscr);
+      }
+      // lookahead rows c1 .. ib2 (c1 = max(1, ib-(p-1)nb), 1-based) after the remaining rows of
+      // the previous block (ab2rht.f90:321: depend(in: B(3,3)))
+      const int c1 = std::max(0, P.ib(o) - P.stride);
+      if (!serial) cudaStreamWaitEvent(sA, evRest, 0);
+      GeoS1Right gl{P, VRc[s], TR[s], o};
+      gl.row_lo = c1;
+      gl.row_hi = P.ib2(o);
+      launch_apply_right(B, ldb, c1, P.ib2(o), gl, sA);
+      if (P.nb2(o) > nb) {
+        count_launch();
+        k_s1_zero_fill<<<nb, 128, 0, sA>>>(B, ldb, P.ib(o), P.ib2(o), nb);
+      }
+      if (c1 > 0) {
+        if (!serial) {
+          cudaEventRecord(evLA, sA);
+          cudaStreamWaitEvent(sB, evLA, 0);
+        }
+        GeoS1Right gr{P, VRc[s], TR[s], o};
+        gr.row_lo = 0;
+        gr.row_hi = c1 - 1;
+        launch_apply_right(B, ldb, 0, c1 - 1, gr, sB);
+        if (!serial) cudaEventRecord(evRest, sB);
+      }
+    }
+    if (timer) timer->mark(sA, 2);
+    if (!serial) {
+      cudaEventRecord(evChain, sA);
+      cudaStreamWaitEvent(sC, evChain, 0);
+      cudaStreamWaitEvent(sA, evAL, 0);  // left update of A done before its right update
+    }
+    launch_apply_right(A, lda, 0, n - 1, GeoS1Right{P, VRc[s], TR[s], -1}, sA);
+    launch_apply_right(Z, ldz, 0, n - 1, GeoS1Right{P, VRc[s], TR[s], -1}, sC);
+    if (!serial) cudaEventRecord(evZ[s], sC);
+  }
+  if (!serial) {  // join
+    cudaEventRecord(evRest, sB);
+    cudaStreamWaitEvent(sA, evRest, 0);
+    cudaEventRecord(evChain, sC);
+    cudaStreamWaitEvent(sA, evChain, 0);
+  }
+  if (timer) timer->mark(sA, -1);
   return 0;
 }
 

@@ -134,7 +134,7 @@ __global__ void k_s2_form_t(int n, int J, int r, int nq, int nblocks, S2Store S)
   double* G = smt;             // nq*nq
   double* Ts = smt + nq * nq;  // nq*nq
   const int ib = blockIdx.x + 1;
-  const bool isV = blockIdx.y == 1;
+  const bool isV = true;  // TU is built by the chase itself (stage2_chase.cu)
   const double* Vb = (isV ? S.V : S.U) + S.ui(1, 1, ib);
   const double* tau = (isV ? S.tauV : S.tauU) + S.ti(1, ib);
   double* T = (isV ? S.TV : S.TU) + S.tt(ib);
@@ -221,9 +221,10 @@ int s2_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
     cudaMemsetAsync(St.V, 0, sizeof(double) * (size_t)ldu * nq * nz, sg);
     cudaMemsetAsync(St.tauU, 0, sizeof(double) * (size_t)nq * nz, sg);
     cudaMemsetAsync(St.tauV, 0, sizeof(double) * (size_t)nq * nz, sg);
+    cudaMemsetAsync(St.TU, 0, sizeof(double) * (size_t)nq * nq * nz, sg);
     s2_launch_chase(sg, A, lda, B, ldb, n, J, r, nq, St, sync, ctx.sequential_chase, ctx.spin_limit);
     count_launch();
-    k_s2_form_t<<<dim3(nblocks, 2), 128, sizeof(double) * 2 * nq * nq, sg>>>(n, J, r, nq, nblocks, St);
+    k_s2_form_t<<<dim3(nblocks, 1), 128, sizeof(double) * 2 * nq * nq, sg>>>(n, J, r, nq, nblocks, St);
     if (timer) timer->mark(sg, 1);
     if (k > 0 && su != sg) cudaStreamWaitEvent(sg, ctx.ev_b, 0);  // lookahead k after bulk k-1
     GeoS2 g{St, n, J, r, nq, nblocks, kLaRight};

@@ -9,8 +9,20 @@
 // (the window row jb+2r of column jb+r), and steps >= ib+3 of sweep ic-1 touch only columns
 // >= jb+3r-1.  Waiting for "sweep ic-1 has finished step ib+2" therefore reproduces the
 // reference's order on every matrix entry, so the pipelined schedule performs exactly the
-// sequential arithmetic (the sequential mode, one CTA running the sweeps in order, must give
+// sequential arithmetic (the sequential mode, one CTA running the sweeps in order, gives
 // bitwise identical results).
+//
+// Latency: a dependent FP64 instruction costs about 64 cycles on GB300, so every step keeps
+// its small problems in registers/shared memory, uses warp shuffles (groups of 4 lanes per
+// row or column) instead of CTA-wide reductions, and
+//  * applies the delayed left reflectors U(1..ic-1, ib) to an entering column as one compact-WY
+//    block (c <- c - U T^T U^T c; the reference applies them one by one, rht2ht.f90:1466-1482,
+//    :1539-1553 -- same product, other rounding).  The forward triangular factor TU of every
+//    block is built column by column as the sweeps generate its reflectors: sweep ic adds
+//    column ic of TU(:,:,ib) right after generating U(ic, ib) (the result is dlarft's TU,
+//    rht2ht.f90:1599-1603);
+//  * fuses the four right-reflector updates of a step (A and B windows, rows above) into one
+//    pass over independent rows.
 //
 // Synchronisation: per-sweep progress words in global memory (st.release / ld.acquire at GPU
 // scope), a ticket so that sweep ic-1 always starts before sweep ic (no deadlock even when not
@@ -25,116 +37,11 @@
 
 namespace pht {
 
-struct Smem2 {
-  double* red;  // 32
-  double* Bc;   // r x r (ld r)
-  double* q;    // r
-  double* tau;  // r
-};
-
-// c <- (I - tau v v^T) c for one column c (length m, contiguous): dlarf('L', m, 1, ...).
-__device__ void cta_larf_col(int m, const double* v, double tau, double* c, Smem2& s) {
-  if (m <= 0 || tau == 0.0) return;
-  double p = 0.0;
-  for (int i = threadIdx.x; i < m; i += blockDim.x) p = fma(v[i], c[i], p);
-  const double w = block_sum(p, s.red);
-  const double tw = tau * w;
-  for (int i = threadIdx.x; i < m; i += blockDim.x) c[i] = fma(-tw, v[i], c[i]);
-  __syncthreads();
-}
-
-// C (m x nc, ld ldc) <- (I - tau v v^T) C: dlarf('L', m, nc, ...).  One warp per column.
-__device__ void cta_larf_left(int m, int nc, const double* v, double tau, double* C, int ldc) {
-  if (m <= 0 || nc <= 0 || tau == 0.0) return;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int j = warp; j < nc; j += nw) {
-    double* c = C + (size_t)j * ldc;
-    double p = 0.0;
-    for (int i = lane; i < m; i += 32) p = fma(v[i], c[i], p);
-    const double tw = tau * warp_sum(p);
-    for (int i = lane; i < m; i += 32) c[i] = fma(-tw, v[i], c[i]);
-  }
-  __syncthreads();
-}
-
-// C (mr x nc, ld ldc) <- C (I - tau v v^T): dlarf('R', mr, nc, ...).  One thread per row.
-__device__ void cta_larf_right(int mr, int nc, const double* v, double tau, double* C, int ldc) {
-  if (mr <= 0 || nc <= 0 || tau == 0.0) return;
-  for (int i = threadIdx.x; i < mr; i += blockDim.x) {
-    double a0 = 0, a1 = 0;
-    int j = 0;
-    for (; j + 1 < nc; j += 2) {
-      a0 = fma(C[i + (size_t)j * ldc], v[j], a0);
-      a1 = fma(C[i + (size_t)(j + 1) * ldc], v[j + 1], a1);
-    }
-    if (j < nc) a0 = fma(C[i + (size_t)j * ldc], v[j], a0);
-    const double tw = tau * (a0 + a1);
-    for (j = 0; j < nc; ++j) C[i + (size_t)j * ldc] = fma(-tw, v[j], C[i + (size_t)j * ldc]);
-  }
-  __syncthreads();
-}
-
-// DLARFG on (alpha, x[0..m-2] with stride incx); writes beta to *alpha, scales x, returns tau.
-__device__ double cta_larfg(int m, double* alpha, double* x, int incx, Smem2& s) {
-  if (m <= 1) {
-    __syncthreads();
-    return 0.0;
-  }
-  double p = 0.0;
-  for (int i = threadIdx.x; i < m - 1; i += blockDim.x) p = fma(x[(size_t)i * incx], x[(size_t)i * incx], p);
-  const double ss = block_sum(p, s.red);
-  const Reflector h = make_reflector(*alpha, ss);
-  __syncthreads();
-  for (int i = threadIdx.x; i < m - 1; i += blockDim.x) x[(size_t)i * incx] *= h.scal;
-  if (threadIdx.x == 0) *alpha = h.beta;
-  __syncthreads();
-  return h.tau;
-}
-
-// "Opposite" reflector of rht2ht.f90:1499-1508: RQ of the nb x nb block Bc (dgerq2), first row
-// of the orthogonal factor (row 1 of dorgr2's Q = H(1)...H(nb)), then DLARFG on that row.
-// Returns tauV; the reflector tail (entries 2..nb) is left in s.q[1..nb-1].
-__device__ double opposite_reflector(int nb, int r, Smem2& s) {
-  double* Bc = s.Bc;
-  const int t = threadIdx.x;
-  for (int i = nb - 1; i >= 0; --i) {  // dgerq2: rows bottom to top
-    double p = 0.0;
-    for (int c = t; c < i; c += blockDim.x) p = fma(Bc[i + c * r], Bc[i + c * r], p);
-    const double ss = block_sum(p, s.red);
-    const Reflector h = make_reflector(Bc[i + i * r], ss);
-    __syncthreads();
-    for (int c = t; c < i; c += blockDim.x) Bc[i + c * r] *= h.scal;
-    __syncthreads();
-    if (h.tau != 0.0) {
-      for (int rho = t; rho < i; rho += blockDim.x) {
-        double w = Bc[rho + i * r];
-        for (int c = 0; c < i; ++c) w = fma(Bc[rho + c * r], Bc[i + c * r], w);
-        const double tw = h.tau * w;
-        for (int c = 0; c < i; ++c) Bc[rho + c * r] = fma(-tw, Bc[i + c * r], Bc[rho + c * r]);
-        Bc[rho + i * r] -= tw;
-      }
-    }
-    __syncthreads();
-    if (t == 0) {
-      Bc[i + i * r] = h.beta;
-      s.tau[i] = h.tau;
-    }
-    __syncthreads();
-  }
-  for (int c = t; c < nb; c += blockDim.x) s.q[c] = (c == 0) ? 1.0 : 0.0;
-  __syncthreads();
-  for (int i = 0; i < nb; ++i) {
-    const double ti = s.tau[i];
-    if (ti != 0.0) {
-      double p = 0.0;
-      for (int c = t; c <= i; c += blockDim.x) p = fma(s.q[c], (c == i) ? 1.0 : Bc[i + c * r], p);
-      const double w = block_sum(p, s.red);
-      const double tw = ti * w;
-      for (int c = t; c <= i; c += blockDim.x) s.q[c] = fma(-tw, (c == i) ? 1.0 : Bc[i + c * r], s.q[c]);
-      __syncthreads();
-    }
-  }
-  return cta_larfg(nb, &s.q[0], &s.q[1], 1, s);
+template <int G>
+PHT_DEV double gsum(double v) {
+#pragma unroll
+  for (int o = 1; o < G; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
 }
 
 PHT_DEV int ld_acquire(const int* p) {
@@ -164,6 +71,21 @@ struct ChaseArgs {
   int pipelined;
 };
 
+// Shared memory of one sweep CTA (r <= 64, nq <= 64).
+struct Sm {
+  double* Bc;   // r x r (ld r+1): the RQ'd B block
+  double* y;    // nq       : U^T c / T^T y
+  double* z;    // nq
+  double* d;    // r        : per-row dot products
+  double* q;    // r        : first row of the RQ orthogonal factor
+  double* tau;  // r
+  double* sc;   // 8 scalars
+  double* red;  // 32
+  int* abort_flag;
+};
+
+constexpr int kChaseMaxThreads = 256;
+
 // Waits until sweep ic-1 has completed step `need`; returns false if the wait was abandoned.
 __device__ bool wait_prev(const ChaseArgs& a, int ic, int need, int* abort_flag) {
   if (!a.pipelined || ic <= 1) return true;
@@ -180,7 +102,7 @@ __device__ bool wait_prev(const ChaseArgs& a, int ic, int need, int* abort_flag)
         ok = 0;
         break;
       }
-      __nanosleep(128);
+      __nanosleep(64);
     }
     *abort_flag = !ok;
   }
@@ -195,12 +117,227 @@ __device__ void publish(const ChaseArgs& a, int ic, int step) {
   if (threadIdx.x == 0) st_release(&a.sync.prog[ic], step);
 }
 
+// c <- H_{m}...H_1 c = c - U T^T U^T c for the first m reflectors of block `ib` (forward
+// T = TU(:,:,ib), reflector i stored at U(i:, i, ib), column frame: row f+i-1 of the block is
+// entry i-1 of U's column).  c points at the matrix entry of block row 1 (row jb_blk+1);
+// `len` limits the rows that exist (n).  All threads participate.
+__device__ void apply_delayed_left(const S2Store& S, int ib, int m, double* c, int len, Sm& s) {
+  if (m <= 0 || len <= 0) return;
+  const int t = threadIdx.x, nt = blockDim.x;
+  const double* U = S.U + S.ui(1, 1, ib);
+  const double* T = S.TU + S.tt(ib);
+  const int ldu = S.ldu, nq = S.nq;
+  // y_j = u_j . c  (u_j nonzero on frame rows j .. j+r-1), 4 lanes per j; uniform loop bounds
+  // so that every lane takes part in the shuffles
+  for (int base = 0; base < m; base += nt / 4) {
+    const int j = base + t / 4, part = t % 4;
+    double acc = 0.0;
+    if (j < m) {
+      const int hi = min(len, ldu);  // frame rows of the block: 0 .. ldu-1
+      for (int i = j + part; i < hi; i += 4) acc = fma(U[i + (size_t)j * ldu], c[i], acc);
+    }
+    acc = gsum<4>(acc);
+    if (part == 0 && j < m) s.y[j] = acc;
+  }
+  __syncthreads();
+  // z = T^T y :  z_j = sum_{l<=j} T[l][j] y_l
+  for (int j = t; j < m; j += nt) {
+    double acc = 0.0;
+    for (int l = 0; l <= j; ++l) acc = fma(T[l + (size_t)j * nq], s.y[l], acc);
+    s.z[j] = acc;
+  }
+  __syncthreads();
+  // c -= U z  (row i gets contributions from reflectors j with j <= i < j + r)
+  for (int i = t; i < len; i += nt) {
+    double acc = 0.0;
+    const int jlo = max(0, i - S.ldu + 1), jhi = min(m - 1, i);
+    for (int j = jlo; j <= jhi; ++j) acc = fma(U[i + (size_t)j * ldu], s.z[j], acc);
+    c[i] -= acc;
+  }
+  __syncthreads();
+}
+
+// Column ic of the forward T of block ib: T[0:ic-1, ic-1] = -tau * T_prev (U_prev^T u_ic),
+// T[ic-1][ic-1] = tau (dlarft 'F','C').  u_ic = U(:, ic, ib) (already stored).
+__device__ void add_t_column(const S2Store& S, int ib, int ic, double tau, int len, Sm& s) {
+  const int t = threadIdx.x, nt = blockDim.x;
+  const double* U = S.U + S.ui(1, 1, ib);
+  double* T = S.TU + S.tt(ib);
+  const int ldu = S.ldu, nq = S.nq, m = ic - 1;
+  const double* u = U + (size_t)m * ldu;
+  for (int base = 0; base < m; base += nt / 4) {  // y_j = u_j . u_m, j < m
+    const int j = base + t / 4, part = t % 4;
+    double acc = 0.0;
+    if (j < m) {
+      const int hi = min(len, ldu);  // frame rows of the block: 0 .. ldu-1
+      for (int i = m + part; i < hi; i += 4) acc = fma(U[i + (size_t)j * ldu], u[i], acc);
+    }
+    acc = gsum<4>(acc);
+    if (part == 0 && j < m) s.y[j] = acc;
+  }
+  __syncthreads();
+  for (int l = t; l < m; l += nt) {
+    double acc = 0.0;
+    for (int q = l; q < m; ++q) acc = fma(T[l + (size_t)q * nq], s.y[q], acc);
+    T[l + (size_t)m * nq] = -tau * acc;
+  }
+  if (t == 0) T[m + (size_t)m * nq] = tau;
+  for (int l = m + 1 + t; l < nq; l += nt) T[l + (size_t)m * nq] = 0.0;
+  __syncthreads();
+}
+
+// DLARFG on the contiguous column x[0..m-1] (alpha = x[0]); 4-lane groups across the CTA.
+// Writes beta to x[0], the scaled tail to x[1..], returns tau (same value in every thread).
+__device__ double larfg_col(int m, double* x, Sm& s) {
+  if (m <= 1) {
+    __syncthreads();
+    return 0.0;
+  }
+  const int t = threadIdx.x, nt = blockDim.x;
+  double p = 0.0;
+  for (int i = 1 + t; i < m; i += nt) p = fma(x[i], x[i], p);
+  p = gsum<32>(p);
+  const int w = t >> 5, lane = t & 31;
+  if (lane == 0) s.red[w] = p;
+  __syncthreads();
+  double ss = 0.0;
+  for (int k = 0; k < (nt >> 5); ++k) ss += s.red[k];
+  const Reflector h = make_reflector(x[0], ss);
+  __syncthreads();
+  for (int i = 1 + t; i < m; i += nt) x[i] *= h.scal;
+  if (t == 0) x[0] = h.beta;
+  __syncthreads();
+  return h.tau;
+}
+
+// C (m x nc, ld ldc) <- (I - tau v v^T) C (dlarf 'L'): 4 lanes per column.
+__device__ void larf_left(int m, int nc, const double* v, double tau, double* C, int ldc) {
+  if (m <= 0 || nc <= 0 || tau == 0.0) {
+    __syncthreads();
+    return;
+  }
+  const int t = threadIdx.x, nt = blockDim.x;
+  for (int base = 0; base < nc; base += nt / 4) {
+    const int j = base + t / 4, part = t % 4;
+    double acc = 0.0;
+    if (j < nc)
+      for (int i = part; i < m; i += 4) acc = fma(v[i], C[i + (size_t)j * ldc], acc);
+    acc = gsum<4>(acc);
+    if (j < nc) {
+      const double tw = tau * acc;
+      for (int i = part; i < m; i += 4) C[i + (size_t)j * ldc] = fma(-tw, v[i], C[i + (size_t)j * ldc]);
+    }
+  }
+  __syncthreads();
+}
+
+// Up to four row ranges updated by the same right reflector (dlarf 'R'): 4 lanes per row.
+struct RightJob {
+  double* C;
+  int ld, rows;
+};
+__device__ void larf_right4(const RightJob* jobs, int njobs, int nc, const double* v, double tau) {
+  if (nc <= 0 || tau == 0.0) {
+    __syncthreads();
+    return;
+  }
+  const int t = threadIdx.x, nt = blockDim.x;
+  int total = 0;
+  for (int k = 0; k < njobs; ++k) total += max(0, jobs[k].rows);
+  for (int base = 0; base < total; base += nt / 4) {
+    int e = base + t / 4;
+    const int part = t % 4;
+    double* C = nullptr;
+    int ld = 0;
+    bool valid = e < total;
+    if (valid) {
+      for (int k = 0; k < njobs; ++k) {
+        const int rk = max(0, jobs[k].rows);
+        if (e < rk) {
+          C = jobs[k].C + e;
+          ld = jobs[k].ld;
+          break;
+        }
+        e -= rk;
+      }
+    }
+    double acc = 0.0;
+    if (valid)
+      for (int j = part; j < nc; j += 4) acc = fma(C[(size_t)j * ld], v[j], acc);
+    acc = gsum<4>(acc);
+    if (valid) {
+      const double tw = tau * acc;
+      for (int j = part; j < nc; j += 4) C[(size_t)j * ld] = fma(-tw, v[j], C[(size_t)j * ld]);
+    }
+  }
+  __syncthreads();
+}
+
+// "Opposite" reflector of rht2ht.f90:1499-1508: RQ (dgerq2) of the nb x nb block in s.Bc,
+// first row q of the orthogonal factor (row 1 of dorgr2's H(1)...H(nb)), DLARFG on q.
+// Returns tauV; the reflector tail (entries 2..nb) is left in s.q[1..nb-1].
+__device__ double opposite_reflector(int nb, int ldb, Sm& s) {
+  double* Bc = s.Bc;
+  const int t = threadIdx.x, nt = blockDim.x;
+  const int rho = t / 4, part = t % 4;  // 4 lanes per row; nt/4 >= r rows
+  for (int i = nb - 1; i >= 0; --i) {
+    double acc = 0.0;
+    if (rho <= i)
+      for (int c = part; c < i; c += 4) acc = fma(Bc[rho + c * ldb], Bc[i + c * ldb], acc);
+    acc = gsum<4>(acc);
+    if (part == 0 && rho <= i) s.d[rho] = acc;
+    if (rho == i && part == 0) {
+      const Reflector h = make_reflector(Bc[i + i * ldb], acc);
+      s.sc[0] = h.tau;
+      s.sc[1] = h.scal;
+      s.sc[2] = h.beta;
+    }
+    __syncthreads();
+    const double ti = s.sc[0], scal = s.sc[1], beta = s.sc[2];
+    if (rho < i && ti != 0.0) {
+      const double w = Bc[rho + i * ldb] + scal * s.d[rho];
+      const double tw = ti * w, tws = tw * scal;
+      for (int c = part; c < i; c += 4) Bc[rho + c * ldb] = fma(-tws, Bc[i + c * ldb], Bc[rho + c * ldb]);
+      if (part == 0) Bc[rho + i * ldb] -= tw;
+    }
+    __syncthreads();
+    if (rho == i) {
+      for (int c = part; c < i; c += 4) Bc[i + c * ldb] *= scal;
+      if (part == 0) {
+        Bc[i + i * ldb] = beta;
+        s.tau[i] = ti;
+      }
+    }
+  }
+  __syncthreads();
+  // q = e1^T H(1) H(2) ... H(nb): one warp, lane c holds q[c] (nb <= 64 -> 2 per lane)
+  if (t < 32) {
+    double q0 = (t == 0) ? 1.0 : 0.0, q1 = 0.0;  // q[t], q[t+32]
+    for (int i = 0; i < nb; ++i) {
+      const double ti = s.tau[i];
+      if (ti == 0.0) continue;
+      // v_i = [Bc(i, 0:i-1), 1, 0...]
+      const double v0 = (t < i) ? Bc[i + t * ldb] : (t == i ? 1.0 : 0.0);
+      const double v1 = (t + 32 < i) ? Bc[i + (t + 32) * ldb] : (t + 32 == i ? 1.0 : 0.0);
+      const double w = gsum<32>(fma(q0, v0, q1 * v1));
+      const double tw = ti * w;
+      q0 = fma(-tw, v0, q0);
+      q1 = fma(-tw, v1, q1);
+    }
+    if (t < nb) s.q[t] = q0;
+    if (t + 32 < nb) s.q[t + 32] = q1;
+  }
+  __syncthreads();
+  return larfg_col(nb, s.q, s);
+}
+
 // One sweep: rht2ht.f90:1452-1594 for column jc = J + ic - 1.
-__device__ void run_sweep(const ChaseArgs& a, int ic, Smem2& s, int* abort_flag) {
+__device__ void run_sweep(const ChaseArgs& a, int ic, Sm& s) {
   double* A = a.A;
   double* B = a.B;
   const int lda = a.lda, ldb = a.ldb, n = a.n, J = a.J, r = a.r, nq = a.nq;
   const S2Store& S = a.S;
+  const int ldbc = r + 1;
 #define A1(i, j) A[(size_t)((i)-1) + (size_t)((j)-1) * lda]
 #define B1(i, j) B[(size_t)((i)-1) + (size_t)((j)-1) * ldb]
   const int t = threadIdx.x;
@@ -208,14 +345,12 @@ __device__ void run_sweep(const ChaseArgs& a, int ic, Smem2& s, int* abort_flag)
   const int jc = J + ic - 1;
   int nb = min(r, n - jc);
   int istart = J + 1;
-  if (!wait_prev(a, ic, min(1 + 2, last_prev), abort_flag)) return;
-  // delayed left reflectors of this group on B(J+i.., jc+r) and A(J+i.., jc) (:1466-1482)
-  if (jc + r <= n)
-    for (int i = 1; i <= ic - 1; ++i) cta_larf_col(r, S.U + S.ui(i, i, 1), S.tauU[S.ti(i, 1)], &B1(J + i, jc + r), s);
-  for (int i = 1; i <= ic - 1; ++i)
-    if (jc <= n) cta_larf_col(min(r, n - J - i + 1), S.U + S.ui(i, i, 1), S.tauU[S.ti(i, 1)], &A1(J + i, jc), s);
+  if (!wait_prev(a, ic, min(1 + 2, last_prev), s.abort_flag)) return;
+  // delayed left reflectors U(1..ic-1, 1) on B(J+1.., jc+r) and A(J+1.., jc) (:1466-1482)
+  if (jc + r <= n) apply_delayed_left(S, 1, ic - 1, &B1(J + 1, jc + r), min(n - J, r + ic - 2), s);
+  if (jc <= n) apply_delayed_left(S, 1, ic - 1, &A1(J + 1, jc), min(n - J, r + ic - 2), s);
   if (nb >= 2) {
-    const double tu = cta_larfg(nb, &A1(jc + 1, jc), &A1(jc + 2, jc), 1, s);  // :1487
+    const double tu = larfg_col(nb, &A1(jc + 1, jc), s);  // :1487
     double* u = S.U + S.ui(ic, ic, 1);
     for (int i = 2 + t; i <= nb; i += blockDim.x) {
       u[i - 1] = A1(jc + i, jc);
@@ -226,10 +361,12 @@ __device__ void run_sweep(const ChaseArgs& a, int ic, Smem2& s, int* abort_flag)
       S.tauU[S.ti(ic, 1)] = tu;
     }
     __syncthreads();
-    cta_larf_left(nb, nb, u, tu, &B1(jc + 1, jc + 1), ldb);  // :1495
-    for (int e = t; e < nb * nb; e += blockDim.x) s.Bc[(e % nb) + (e / nb) * r] = B1(jc + 1 + e % nb, jc + 1 + e / nb);
+    add_t_column(S, 1, ic, tu, min(n - J, r + nq), s);
+    larf_left(nb, nb, u, tu, &B1(jc + 1, jc + 1), ldb);  // :1495
+    for (int e = t; e < nb * nb; e += blockDim.x)
+      s.Bc[(e % nb) + (e / nb) * ldbc] = B1(jc + 1 + e % nb, jc + 1 + e / nb);
     __syncthreads();
-    const double tv = opposite_reflector(nb, r, s);  // :1499-1508
+    const double tv = opposite_reflector(nb, ldbc, s);  // :1499-1508
     double* v = S.V + S.ui(ic, ic, 1);
     for (int i = 2 + t; i <= nb; i += blockDim.x) v[i - 1] = s.q[i - 1];
     if (t == 0) {
@@ -237,29 +374,34 @@ __device__ void run_sweep(const ChaseArgs& a, int ic, Smem2& s, int* abort_flag)
       S.tauV[S.ti(ic, 1)] = tv;
     }
     __syncthreads();
-    cta_larf_right(min(n, jc + r + nb) - jc, nb, v, tv, &A1(jc + 1, jc + 1), lda);  // :1510
-    cta_larf_right(nb, nb, v, tv, &B1(jc + 1, jc + 1), ldb);                          // :1513
+    {
+      // :1510, :1513, :1518, :1520 -- one reflector, four row ranges
+      RightJob jobs[4] = {{&A1(jc + 1, jc + 1), lda, min(n, jc + r + nb) - jc},
+                          {&B1(jc + 1, jc + 1), ldb, nb},
+                          {&A1(istart, jc + 1), lda, jc - istart + 1},
+                          {&B1(istart, jc + 1), ldb, jc - istart + 1}};
+      larf_right4(jobs, 4, nb, v, tv);
+    }
     for (int i = 2 + t; i <= nb; i += blockDim.x) B1(jc + i, jc + 1) = 0.0;
     __syncthreads();
-    cta_larf_right(jc - istart + 1, nb, v, tv, &A1(istart, jc + 1), lda);  // :1518
-    cta_larf_right(jc - istart + 1, nb, v, tv, &B1(istart, jc + 1), ldb);  // :1520
+  } else if (ic <= nq) {
+    // no reflector in this column: keep TU's column ic consistent (tau = 0)
+    add_t_column(S, 1, ic, 0.0, min(n - J, r + nq), s);
   }
   publish(a, ic, 1);
   if (nb < 2) return;  // :1484 skips the chase
   for (int jb = jc + 1; jb <= n; jb += r) {  // :1528
     const int ib = (jb - (jc + 1)) / r + 2;
-    if (!wait_prev(a, ic, min(ib + 2, last_prev), abort_flag)) return;
+    if (!wait_prev(a, ic, min(ib + 2, last_prev), s.abort_flag)) return;
     nb = min(r, n - jb - r + 1);
     istart = max(J + 1, J + 1 + (ib - 1) * r - (nq - ic) * r);
-    if (jb + r + r - 1 <= n)  // :1539-1544
-      for (int i = 1; i <= ic - 1; ++i)
-        cta_larf_col(r, S.U + S.ui(i, i, ib), S.tauU[S.ti(i, ib)], &B1(jb + r - ic + i, jb + r + r - 1), s);
-    for (int i = 1; i <= ic - 1; ++i)  // :1550-1553
-      if (jb + r - ic + i <= n)
-        cta_larf_col(min(r, n - (jb + r - ic + i) + 1), S.U + S.ui(i, i, ib), S.tauU[S.ti(i, ib)],
-                     &A1(jb + r - ic + i, jb), s);
+    const int jbb = J + (ib - 1) * r;  // block frame: reflector i of block ib starts at row jbb+i
+    if (jb + r + r - 1 <= n)           // :1539-1544
+      apply_delayed_left(S, ib, ic - 1, &B1(jbb + 1, jb + r + r - 1), min(n - jbb, r + ic - 2), s);
+    if (jb + r - ic + 1 <= n)  // :1550-1553
+      apply_delayed_left(S, ib, ic - 1, &A1(jbb + 1, jb), min(n - jbb, r + ic - 2), s);
     if (nb >= 2) {
-      const double tu = cta_larfg(nb, &A1(jb + r, jb), &A1(jb + r + 1, jb), 1, s);  // :1558
+      const double tu = larfg_col(nb, &A1(jb + r, jb), s);  // :1558
       double* u = S.U + S.ui(ic, ic, ib);
       for (int i = 1 + t; i <= nb - 1; i += blockDim.x) {
         u[i] = A1(jb + r + i, jb);
@@ -270,11 +412,12 @@ __device__ void run_sweep(const ChaseArgs& a, int ic, Smem2& s, int* abort_flag)
         S.tauU[S.ti(ic, ib)] = tu;
       }
       __syncthreads();
-      cta_larf_left(nb, nb, u, tu, &B1(jb + r, jb + r), ldb);  // :1566
+      add_t_column(S, ib, ic, tu, min(n - jbb, r + nq), s);
+      larf_left(nb, nb, u, tu, &B1(jb + r, jb + r), ldb);  // :1566
       for (int e = t; e < nb * nb; e += blockDim.x)
-        s.Bc[(e % nb) + (e / nb) * r] = B1(jb + r + e % nb, jb + r + e / nb);
+        s.Bc[(e % nb) + (e / nb) * ldbc] = B1(jb + r + e % nb, jb + r + e / nb);
       __syncthreads();
-      const double tv = opposite_reflector(nb, r, s);  // :1570-1579
+      const double tv = opposite_reflector(nb, ldbc, s);  // :1570-1579
       double* v = S.V + S.ui(ic, ic, ib);
       for (int i = 2 + t; i <= nb; i += blockDim.x) v[i - 1] = s.q[i - 1];
       if (t == 0) {
@@ -282,12 +425,18 @@ __device__ void run_sweep(const ChaseArgs& a, int ic, Smem2& s, int* abort_flag)
         S.tauV[S.ti(ic, ib)] = tv;
       }
       __syncthreads();
-      cta_larf_right(min(n, jb + 2 * r + nb - 1) - jb - r + 1, nb, v, tv, &A1(jb + r, jb + r), lda);  // :1581
-      cta_larf_right(nb, nb, v, tv, &B1(jb + r, jb + r), ldb);                                        // :1584
+      {
+        // :1581, :1584, :1589, :1591
+        RightJob jobs[4] = {{&A1(jb + r, jb + r), lda, min(n, jb + 2 * r + nb - 1) - jb - r + 1},
+                            {&B1(jb + r, jb + r), ldb, nb},
+                            {&A1(istart, jb + r), lda, jb + r - istart},
+                            {&B1(istart, jb + r), ldb, jb + r - istart}};
+        larf_right4(jobs, 4, nb, v, tv);
+      }
       for (int i = 1 + t; i <= nb - 1; i += blockDim.x) B1(jb + r + i, jb + r) = 0.0;
       __syncthreads();
-      cta_larf_right(jb + r - istart, nb, v, tv, &A1(istart, jb + r), lda);  // :1589
-      cta_larf_right(jb + r - istart, nb, v, tv, &B1(istart, jb + r), ldb);  // :1591
+    } else if (jbb < n) {
+      add_t_column(S, ib, ic, 0.0, min(n - jbb, r + nq), s);
     }
     publish(a, ic, ib);
   }
@@ -295,25 +444,29 @@ __device__ void run_sweep(const ChaseArgs& a, int ic, Smem2& s, int* abort_flag)
 #undef B1
 }
 
-constexpr int kChaseThreads = 256;
-
-__global__ void __launch_bounds__(kChaseThreads) k_s2_chase(ChaseArgs a) {
+__global__ void __launch_bounds__(kChaseMaxThreads, 1) k_s2_chase(ChaseArgs a) {
   extern __shared__ double sm[];
   __shared__ int s_ic, s_abort;
-  Smem2 s;
-  s.red = sm;
-  s.Bc = sm + 32;
-  s.q = s.Bc + a.r * a.r;
-  s.tau = s.q + a.r;
+  const int r = a.r, nq = a.nq;
+  Sm s;
+  s.Bc = sm;
+  s.y = s.Bc + (size_t)r * (r + 1);
+  s.z = s.y + nq;
+  s.d = s.z + nq;
+  s.q = s.d + r;
+  s.tau = s.q + r;
+  s.sc = s.tau + r;
+  s.red = s.sc + 8;
+  s.abort_flag = &s_abort;
   if (threadIdx.x == 0) s_abort = 0;
   if (!a.pipelined) {
     __syncthreads();
-    for (int ic = 1; ic <= a.nq; ++ic) run_sweep(a, ic, s, &s_abort);
+    for (int ic = 1; ic <= a.nq; ++ic) run_sweep(a, ic, s);
     return;
   }
   if (threadIdx.x == 0) s_ic = atomicAdd(a.sync.ticket, 1) + 1;
   __syncthreads();
-  run_sweep(a, s_ic, s, &s_abort);
+  run_sweep(a, s_ic, s);
 }
 
 void s2_launch_chase(cudaStream_t st, double* A, int lda, double* B, int ldb, int n, int J, int r, int nq,
@@ -331,13 +484,18 @@ void s2_launch_chase(cudaStream_t st, double* A, int lda, double* B, int ldb, in
   a.sync = sync;
   a.spin_limit = spin_limit;
   a.pipelined = sequential ? 0 : 1;
-  const size_t smem = sizeof(double) * (32 + (size_t)r * r + 2 * r + 8);
+  // 4 lanes per row of the r x r block (the RQ needs nt/4 >= r), at least two warps
+  const int rows = ((r > nq ? r : nq) + 7) / 8 * 8;
+  int nt = 4 * rows;
+  if (nt < 64) nt = 64;
+  if (nt > kChaseMaxThreads) nt = kChaseMaxThreads;
+  const size_t smem = sizeof(double) * ((size_t)r * (r + 1) + 2 * (size_t)nq + 3 * (size_t)r + 8 + 32);
   if (a.pipelined) {
     cudaMemsetAsync(sync.prog, 0, sizeof(int) * (nq + 1), st);
     cudaMemsetAsync(sync.ticket, 0, sizeof(int), st);
   }
   count_launch();
-  k_s2_chase<<<a.pipelined ? nq : 1, kChaseThreads, smem, st>>>(a);
+  k_s2_chase<<<a.pipelined ? nq : 1, nt, smem, st>>>(a);
 }
 
 }  // namespace pht
