@@ -9,6 +9,7 @@
 #include "launch_count.h"
 #include "paraht_impl.h"
 #include "paraht_internal.cuh"
+#include "split_apply.cuh"
 
 namespace pht {
 thread_local long long tl_launches = 0;
@@ -38,6 +39,24 @@ void* Ctx::workspace(size_t bytes) {
   }
   ws_bytes = want;
   return ws;
+}
+
+void* Ctx::split_region(int r, int ops, size_t op_bytes) {
+  const size_t per = ((size_t)ops * op_bytes + 255) & ~(size_t)255;
+  if (per > sws_region) {
+    cudaDeviceSynchronize();  // regions may be in use by queued work on any stream
+    if (sws) cudaFree(sws);
+    sws = nullptr;
+    sws_region = 0;
+    if (cudaMalloc(&sws, 6 * per) != cudaSuccess) {
+      cudaGetLastError();
+      sws = nullptr;
+      return nullptr;
+    }
+    sws_region = per;
+    sws_bytes = 6 * per;
+  }
+  return (char*)sws + (size_t)r * sws_region;
 }
 
 int Ctx::ensure_staging(size_t bytes_each) {
@@ -256,7 +275,11 @@ static int run_device(Ctx& x, int which, int n, double* A, int lda, double* B, i
                       int ldz, int r, int p, int nq, int flags) {
   x.launches = 0;
   if (n == 0) return 0;
-  if (flags & PARAHT_FLAG_SPLIT) return PARAHT_ERR_NOT_SUPPORTED;
+  x.split = (flags & PARAHT_FLAG_SPLIT) ? 1 : 0;
+  if (x.split) {  // size the per-op operand slots once for both stages
+    const int ops = std::max(n / std::max(1, (p - 1) * r) + 2, n / std::max(1, r) + 4);
+    if (!x.split_region(0, ops, sizeof(pht::SplitOpData))) return PARAHT_ERR_ALLOC;
+  }
   const long long launches0 = pht::tl_launches;
   const bool timed = flags & PARAHT_FLAG_TIME_COMPONENTS;
   if (flags & PARAHT_FLAG_CHECK_FINITE) {

@@ -65,6 +65,12 @@ struct Ctx {
   double phase[8] = {0};
   double residue[2] = {0};
   long long launches = 0;  // kernels launched by the last call
+  int split = 0;           // split-precision bulk updates (PARAHT_FLAG_SPLIT)
+  void* sws = nullptr;     // split-precision per-op operand slots
+  size_t sws_bytes = 0;
+  size_t sws_region = 0;   // bytes per region (one region per launch site)
+  // Returns region r of the split workspace, sized for `ops` ops of `op_bytes` each (6 regions).
+  void* split_region(int r, int ops, size_t op_bytes);
   double* dresidue = nullptr;
   void* workspace(size_t bytes);
   int ensure_staging(size_t bytes_each);

@@ -46,6 +46,14 @@ PHT_DEV double block_sum(double v, double* red) {
 // of x, returns tau and the scale factor 1/(alpha-beta) for x; beta replaces alpha.
 // Computed redundantly by every thread from identical inputs (bitwise identical results), so no
 // broadcast is needed.  tau = 0 (identity) when x == 0, as in DLARFG.
+//
+// The scalars are formed from one reciprocal square root and one reciprocal, because every
+// dependent FP64 instruction costs about 64 cycles on GB300 and this sits on the critical path
+// of every chain:  s = alpha^2 + |x|^2,  rho = 1/sqrt(s),  |beta| = s*rho,
+//   tau  = (beta - alpha)/beta = 1 + |alpha| rho,
+//   scal = 1/(alpha - beta)    = sign(alpha) / (|alpha| + |beta|).
+// Unlike DLARFG there is no rescaling loop for |beta| below the safe minimum: entries smaller
+// than about 1e-154 (whose squares underflow) are treated as zero.
 struct Reflector {
   double tau, scal, beta;
 };
@@ -57,11 +65,13 @@ PHT_DEV Reflector make_reflector(double alpha, double xnorm2) {
     h.beta = alpha;
     return h;
   }
-  const double xnorm = sqrt(xnorm2);
-  const double beta = -copysign(hypot(alpha, xnorm), alpha);
-  h.tau = (beta - alpha) / beta;
-  h.scal = 1.0 / (alpha - beta);
-  h.beta = beta;
+  const double s = fma(alpha, alpha, xnorm2);
+  const double rho = rsqrt(s);
+  const double nrm = s * rho;
+  const double aa = fabs(alpha);
+  h.beta = -copysign(nrm, alpha);
+  h.tau = fma(aa, rho, 1.0);
+  h.scal = copysign(1.0 / (aa + nrm), alpha);
   return h;
 }
 

@@ -18,6 +18,7 @@
 #include "paraht_internal.cuh"
 #include "paraht_impl.h"
 #include "stage1_geom.cuh"
+#include "split_apply.cuh"
 #include "wy_apply.cuh"
 
 namespace pht {
@@ -399,6 +400,15 @@ int s1_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
   if (!fast_l) cudaFuncSetAttribute(k_s1_left_gen, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsm);
   if (!fast_r) cudaFuncSetAttribute(k_s1_right_gen, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm);
 
+  // split-precision bulk updates (split_apply.cuh) where the op shapes fit; one operand region
+  // per launch site: 0 B left, 1 A left, 2 Q, 3 remaining B rows, 4 A right, 5 Z right
+  const bool sp = ctx.split && split_fits(nb, L);
+  void* reg[6] = {};
+  if (sp)
+    for (int i = 0; i < 6; ++i) {
+      reg[i] = ctx.split_region(i, (int)nblk0, sizeof(SplitOpData));
+      if (!reg[i]) return PARAHT_ERR_ALLOC;
+    }
   cudaEvent_t evL = ctx.ev[0], evAL = ctx.ev[1], evLA = ctx.ev[2], evRest = ctx.ev[3], evChain = ctx.ev[4];
   cudaEvent_t evZ[2] = {ctx.ev[5], ctx.ev[6]};
   if (!serial) {  // side streams start after everything already queued on sA
@@ -427,10 +437,10 @@ int s1_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
       cudaStreamWaitEvent(sC, evL, 0);
       cudaStreamWaitEvent(sA, evRest, 0);  // remaining-row B updates of panel k-1 done
     }
-    launch_apply_left(B, ldb, P.ib(P.nblocks - 1), n - 1, GeoS1Left{P, VL[s], TL[s], 0}, sA);
-    launch_apply_left(A, lda, jb0 + nb, n - 1, GeoS1Left{P, VL[s], TL[s], 1}, sC);
+    apply_left_any(reg[0], B, ldb, P.ib(P.nblocks - 1), n - 1, GeoS1Left{P, VL[s], TL[s], 0}, P.nblocks, sA);
+    apply_left_any(reg[1], A, lda, jb0 + nb, n - 1, GeoS1Left{P, VL[s], TL[s], 1}, P.nblocks, sC);
     if (!serial) cudaEventRecord(evAL, sC);
-    launch_apply_right(Q, ldq, 0, n - 1, GeoS1Q{P, VL[s], TL[s]}, sC);
+    apply_right_any(reg[2], Q, ldq, 0, n - 1, GeoS1Q{P, VL[s], TL[s]}, P.nblocks, sC);
     if (timer) timer->mark(sA, 1);
     if (!serial) {
       cudaEventRecord(evLA, sA);  // B left update done: the remaining-row updates may start
@@ -463,7 +473,7 @@ int s1_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
         GeoS1Right gr{P, VRc[s], TR[s], o};
         gr.row_lo = 0;
         gr.row_hi = c1 - 1;
-        launch_apply_right(B, ldb, 0, c1 - 1, gr, sB);
+        apply_right_any(reg[3], B, ldb, 0, c1 - 1, gr, 1, sB);
         if (!serial) cudaEventRecord(evRest, sB);
       }
     }
@@ -473,8 +483,8 @@ int s1_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
       cudaStreamWaitEvent(sC, evChain, 0);
       cudaStreamWaitEvent(sA, evAL, 0);  // left update of A done before its right update
     }
-    launch_apply_right(A, lda, 0, n - 1, GeoS1Right{P, VRc[s], TR[s], -1}, sA);
-    launch_apply_right(Z, ldz, 0, n - 1, GeoS1Right{P, VRc[s], TR[s], -1}, sC);
+    apply_right_any(reg[4], A, lda, 0, n - 1, GeoS1Right{P, VRc[s], TR[s], -1}, P.nblocks, sA);
+    apply_right_any(reg[5], Z, ldz, 0, n - 1, GeoS1Right{P, VRc[s], TR[s], -1}, P.nblocks, sC);
     if (!serial) cudaEventRecord(evZ[s], sC);
   }
   if (!serial) {  // join

@@ -36,6 +36,8 @@ struct GeoS1Left {
   const double* TL;
   int onA;
   PHT_DEV int count() const { return P.nblocks; }
+  PHT_DEV int slot_op(int s) const { return s; }
+  PHT_DEV int op_slot(int o) const { return o; }
   PHT_DEV WYOp op(int o) const {
     WYOp w;
     w.start = P.ib(o);
@@ -57,6 +59,8 @@ struct GeoS1Q {
   const double* VL;
   const double* TL;
   PHT_DEV int count() const { return P.nblocks; }
+  PHT_DEV int slot_op(int s) const { return s; }
+  PHT_DEV int op_slot(int o) const { return o; }
   PHT_DEV WYOp op(int o) const {
     WYOp w;
     w.start = P.ib(o);
@@ -81,6 +85,8 @@ struct GeoS1Right {
   int bl_only;  // -1: all blocks, all rows; else only block bl_only, rows [row_lo, row_hi]
   int row_lo = 0, row_hi = -1;
   PHT_DEV int count() const { return bl_only >= 0 ? 1 : P.nblocks; }
+  PHT_DEV int slot_op(int s) const { return s; }
+  PHT_DEV int op_slot(int o) const { return o; }
   PHT_DEV WYOp op(int i) const {
     const int o = bl_only >= 0 ? bl_only : i;
     WYOp w;

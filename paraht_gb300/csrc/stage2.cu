@@ -18,6 +18,7 @@
 #include "paraht_impl.h"
 #include "paraht_internal.cuh"
 #include "s2_common.cuh"
+#include "split_apply.cuh"
 #include "wy_apply.cuh"
 
 namespace pht {
@@ -44,6 +45,10 @@ struct GeoS2 {
         return nblocks;
     }
   }
+  // Split-precision preparation slots: only the compact-WY ops (kUpRight: the last op of each
+  // block; single reflectors are applied in FP64 by the split kernel and need no slot).
+  PHT_DEV int slot_op(int s) const { return kind == kUpRight ? s * nq + nq - 1 : s; }
+  PHT_DEV int op_slot(int o) const { return kind == kUpRight ? o / nq : o; }
   PHT_DEV WYOp single(int ic, int ib, int rlo1, int rhi1) const {  // 1-based inclusive rows
     const int jb = J + (ib - 1) * r;
     WYOp w;
@@ -211,6 +216,15 @@ int s2_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
     cudaEventRecord(ctx.ev_a, sg);
     cudaStreamWaitEvent(su, ctx.ev_a, 0);
   }
+  // split-precision bulk updates where the op shapes fit (k = nq reflectors, r+nq long);
+  // regions: 0 B right, 1 A right, 2 B left, 3 A left, 4 Q, 5 Z
+  const bool sp = ctx.split && split_fits(nq, r + nq);
+  void* reg[6] = {};
+  if (sp)
+    for (int i = 0; i < 6; ++i) {
+      reg[i] = ctx.split_region(i, nb0, sizeof(SplitOpData));
+      if (!reg[i]) return PARAHT_ERR_ALLOC;
+    }
   int k = 0;
   for (int J = 1; J <= n - 2; J += nq, ++k) {  // rht2ht.f90:1417
     const int nblocks = (n - J + r - 1) / r;
@@ -239,16 +253,18 @@ int s2_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
       cudaEventRecord(ctx.ev_a, sg);
       cudaStreamWaitEvent(su, ctx.ev_a, 0);
     }
+    // bulk updates; in the right update a row can lie in block ib's compact-WY range and in
+    // block ib-1's staircase range, so singles and blocks form one ordered list
     g.kind = kUpRight;
-    launch_apply_right(B, ldb, 0, n - 1, g, su);
-    launch_apply_right(A, lda, 0, n - 1, g, su);
+    apply_right_any(reg[0], B, ldb, 0, n - 1, g, nblocks, su);
+    apply_right_any(reg[1], A, lda, 0, n - 1, g, nblocks, su);
     g.kind = kUpLeft;
-    launch_apply_left(B, ldb, J, n - 1, g, su);
-    launch_apply_left(A, lda, J, n - 1, g, su);
+    apply_left_any(reg[2], B, ldb, J, n - 1, g, nblocks, su);
+    apply_left_any(reg[3], A, lda, J, n - 1, g, nblocks, su);
     g.kind = kUpQ;
-    launch_apply_right(Q, ldq, 0, n - 1, g, su);
+    apply_right_any(reg[4], Q, ldq, 0, n - 1, g, nblocks, su);
     g.kind = kUpZ;
-    launch_apply_right(Z, ldz, 0, n - 1, g, su);
+    apply_right_any(reg[5], Z, ldz, 0, n - 1, g, nblocks, su);
     if (su != sg) cudaEventRecord(ctx.ev_b, su);
   }
   if (su != sg) cudaStreamWaitEvent(sg, ctx.ev_b, 0);

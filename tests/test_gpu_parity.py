@@ -161,3 +161,27 @@ def ph_rht2ht_host(ctx, A, B, Q, Z, r, nq, flags):
     torch.cuda.synchronize()
     for X, D in zip((A, B, Q, Z), dev):
         X[:] = D.cpu().numpy().T
+
+
+@pytest.mark.parametrize("n,r,p,nq,dist", [
+    (100, 16, 2, 8, "std"),
+    (257, 16, 4, 16, "std"),
+    (300, 16, 3, 8, "graded"),
+    (200, 8, 4, 8, "refcompat"),
+])
+def test_split_precision_reduce(oracle, ctx, n, r, p, nq, dist):
+    """Split-precision (emulated FP64 on BF16 tensor cores) bulk updates: backward error and
+    orthogonality <= 1e-13 (the split path's acceptance bound), exact structure, and the same
+    HT pencil as the oracle up to signs."""
+    A0, B0 = make(n, dist)
+    A, B = copies(A0, B0)
+    Q, Z = identity(n), identity(n)
+    ctx.reduce_host(A, B, Q, Z, r, p, nq, flags=ph.PARAHT_FLAG_SPLIT)
+    assert bwd(Q, A0, Z, A) <= 1e-13 and bwd(Q, B0, Z, B) <= 1e-13
+    assert orth(Q) <= 1e-13 and orth(Z) <= 1e-13
+    assert np.all(np.tril(A, -2) == 0.0) and np.all(np.tril(B, -1) == 0.0)
+    if dist != "graded":
+        Ao, Bo, _, _ = oracle_reduce(oracle, A0, B0, r, p, nq)
+        assert abs_rel_max_diff(A, Ao) < 1e-8
+        assert abs_rel_max_diff(B, Bo) < 1e-8
+    assert ctx.launch_count() > 0
