@@ -22,7 +22,9 @@
 //    column ic of TU(:,:,ib) right after generating U(ic, ib) (the result is dlarft's TU,
 //    rht2ht.f90:1599-1603);
 //  * fuses the four right-reflector updates of a step (A and B windows, rows above) into one
-//    pass over independent rows.
+//    pass over independent rows;
+//  * runs eight warps per sweep so that the FP64 updates of a step (rows above the window in
+//    particular) are spread over all four schedulers of the SM.
 //
 // Synchronisation: per-sweep progress words in global memory (st.release / ld.acquire at GPU
 // scope), a ticket so that sweep ic-1 always starts before sweep ic (no deadlock even when not
@@ -82,6 +84,7 @@ struct Sm {
   double* sc;   // 8 scalars
   double* red;  // 32
   int* abort_flag;
+  int ldr;      // leading dimension of Bc (r + 1)
 };
 
 constexpr int kChaseMaxThreads = 256;
@@ -210,27 +213,6 @@ __device__ double larfg_col(int m, double* x, Sm& s) {
   return h.tau;
 }
 
-// C (m x nc, ld ldc) <- (I - tau v v^T) C (dlarf 'L'): 4 lanes per column.
-__device__ void larf_left(int m, int nc, const double* v, double tau, double* C, int ldc) {
-  if (m <= 0 || nc <= 0 || tau == 0.0) {
-    __syncthreads();
-    return;
-  }
-  const int t = threadIdx.x, nt = blockDim.x;
-  for (int base = 0; base < nc; base += nt / 4) {
-    const int j = base + t / 4, part = t % 4;
-    double acc = 0.0;
-    if (j < nc)
-      for (int i = part; i < m; i += 4) acc = fma(v[i], C[i + (size_t)j * ldc], acc);
-    acc = gsum<4>(acc);
-    if (j < nc) {
-      const double tw = tau * acc;
-      for (int i = part; i < m; i += 4) C[i + (size_t)j * ldc] = fma(-tw, v[i], C[i + (size_t)j * ldc]);
-    }
-  }
-  __syncthreads();
-}
-
 // Up to four row ranges updated by the same right reflector (dlarf 'R'): 4 lanes per row.
 struct RightJob {
   double* C;
@@ -278,7 +260,7 @@ __device__ void larf_right4(const RightJob* jobs, int njobs, int nc, const doubl
 // Returns tauV; the reflector tail (entries 2..nb) is left in s.q[1..nb-1].
 __device__ double opposite_reflector(int nb, int ldb, Sm& s) {
   double* Bc = s.Bc;
-  const int t = threadIdx.x, nt = blockDim.x;
+  const int t = threadIdx.x;
   const int rho = t / 4, part = t % 4;  // 4 lanes per row; nt/4 >= r rows
   for (int i = nb - 1; i >= 0; --i) {
     double acc = 0.0;
@@ -331,13 +313,43 @@ __device__ double opposite_reflector(int nb, int ldb, Sm& s) {
   return larfg_col(nb, s.q, s);
 }
 
+// C (m x nc, ld ldc) <- (I - tau v v^T) C (dlarf 'L') by the threads t >= t0 only (t0 a multiple
+// of 32), 4 lanes per column, without a barrier.
+__device__ void larf_left_part(int m, int nc, const double* v, double tau, double* C, int ldc, int t0) {
+  const int t = (int)threadIdx.x - t0, nt = (int)blockDim.x - t0;
+  if (t < 0 || m <= 0 || nc <= 0 || tau == 0.0) return;
+  for (int base = 0; base < nc; base += nt / 4) {
+    const int j = base + t / 4, part = t % 4;
+    double acc = 0.0;
+    if (j < nc)
+      for (int i = part; i < m; i += 4) acc = fma(v[i], C[i + (size_t)j * ldc], acc);
+    acc = gsum<4>(acc);
+    if (j < nc) {
+      const double tw = tau * acc;
+      for (int i = part; i < m; i += 4) C[i + (size_t)j * ldc] = fma(-tw, v[i], C[i + (size_t)j * ldc]);
+    }
+  }
+}
+
+// The B block at Bblk (nb x nb) <- H_u Bblk (rht2ht.f90:1495 / :1566) and the opposite reflector
+// of the product (:1499-1508 / :1570-1579).  Returns tau_v; the reflector tail is in s.q[1..nb-1].
+// (The block is a general matrix here: the sweeps of a group leave fill below its diagonal that
+// later sweeps remove, so the first row of its RQ factor needs the full factorisation.)
+__device__ double left_and_opposite(int nb, const double* u, double tu, double* Bblk, int ldb, Sm& s) {
+  const int t = threadIdx.x, ldr = s.ldr;
+  larf_left_part(nb, nb, u, tu, Bblk, ldb, 0);
+  __syncthreads();
+  for (int e = t; e < nb * nb; e += blockDim.x) s.Bc[(e % nb) + (e / nb) * ldr] = Bblk[(e % nb) + (size_t)(e / nb) * ldb];
+  __syncthreads();
+  return opposite_reflector(nb, ldr, s);
+}
+
 // One sweep: rht2ht.f90:1452-1594 for column jc = J + ic - 1.
 __device__ void run_sweep(const ChaseArgs& a, int ic, Sm& s) {
   double* A = a.A;
   double* B = a.B;
   const int lda = a.lda, ldb = a.ldb, n = a.n, J = a.J, r = a.r, nq = a.nq;
   const S2Store& S = a.S;
-  const int ldbc = r + 1;
 #define A1(i, j) A[(size_t)((i)-1) + (size_t)((j)-1) * lda]
 #define B1(i, j) B[(size_t)((i)-1) + (size_t)((j)-1) * ldb]
   const int t = threadIdx.x;
@@ -362,11 +374,7 @@ __device__ void run_sweep(const ChaseArgs& a, int ic, Sm& s) {
     }
     __syncthreads();
     add_t_column(S, 1, ic, tu, min(n - J, r + nq), s);
-    larf_left(nb, nb, u, tu, &B1(jc + 1, jc + 1), ldb);  // :1495
-    for (int e = t; e < nb * nb; e += blockDim.x)
-      s.Bc[(e % nb) + (e / nb) * ldbc] = B1(jc + 1 + e % nb, jc + 1 + e / nb);
-    __syncthreads();
-    const double tv = opposite_reflector(nb, ldbc, s);  // :1499-1508
+    const double tv = left_and_opposite(nb, u, tu, &B1(jc + 1, jc + 1), ldb, s);  // :1495-1508
     double* v = S.V + S.ui(ic, ic, 1);
     for (int i = 2 + t; i <= nb; i += blockDim.x) v[i - 1] = s.q[i - 1];
     if (t == 0) {
@@ -413,11 +421,7 @@ __device__ void run_sweep(const ChaseArgs& a, int ic, Sm& s) {
       }
       __syncthreads();
       add_t_column(S, ib, ic, tu, min(n - jbb, r + nq), s);
-      larf_left(nb, nb, u, tu, &B1(jb + r, jb + r), ldb);  // :1566
-      for (int e = t; e < nb * nb; e += blockDim.x)
-        s.Bc[(e % nb) + (e / nb) * ldbc] = B1(jb + r + e % nb, jb + r + e / nb);
-      __syncthreads();
-      const double tv = opposite_reflector(nb, ldbc, s);  // :1570-1579
+      const double tv = left_and_opposite(nb, u, tu, &B1(jb + r, jb + r), ldb, s);  // :1566-1579
       double* v = S.V + S.ui(ic, ic, ib);
       for (int i = 2 + t; i <= nb; i += blockDim.x) v[i - 1] = s.q[i - 1];
       if (t == 0) {
@@ -458,6 +462,7 @@ __global__ void __launch_bounds__(kChaseMaxThreads, 1) k_s2_chase(ChaseArgs a) {
   s.sc = s.tau + r;
   s.red = s.sc + 8;
   s.abort_flag = &s_abort;
+  s.ldr = r + 1;
   if (threadIdx.x == 0) s_abort = 0;
   if (!a.pipelined) {
     __syncthreads();
@@ -484,11 +489,9 @@ void s2_launch_chase(cudaStream_t st, double* A, int lda, double* B, int ldb, in
   a.sync = sync;
   a.spin_limit = spin_limit;
   a.pipelined = sequential ? 0 : 1;
-  // 4 lanes per row of the r x r block (the RQ needs nt/4 >= r), at least two warps
-  const int rows = ((r > nq ? r : nq) + 7) / 8 * 8;
-  int nt = 4 * rows;
-  if (nt < 64) nt = 64;
-  if (nt > kChaseMaxThreads) nt = kChaseMaxThreads;
+  // 4 lanes per row of the r x r block (the RQ needs nt/4 >= r); eight warps so that the
+  // right-reflector updates of the rows above the window have lanes to spread over
+  const int nt = kChaseMaxThreads;
   const size_t smem = sizeof(double) * ((size_t)r * (r + 1) + 2 * (size_t)nq + 3 * (size_t)r + 8 + 32);
   if (a.pipelined) {
     cudaMemsetAsync(sync.prog, 0, sizeof(int) * (nq + 1), st);
