@@ -44,6 +44,7 @@ extern "C" {
 #define PARAHT_ERR_NOT_SUPPORTED (-1005) /* parameter combination not supported on this device */
 #define PARAHT_ERR_NO_DEVICE (-1006)     /* no usable CUDA device */
 #define PARAHT_ERR_BAD_CTX (-1007)       /* null or destroyed context */
+#define PARAHT_ERR_TOO_LARGE (-1008)     /* exceeds the fixed scratch of paraht_rht2ht_d_noalloc */
 
 /* ---- flags (bit set) ---- */
 #define PARAHT_FLAG_TIME_COMPONENTS 1 /* record per-phase times (time_components, src/ab2rht.f90:13) */
@@ -99,6 +100,20 @@ int paraht_rht2ht_d(paraht_ctx ctx, int n, double* A, int lda, double* B, int ld
                     int ldz, int r, int nq, int flags);
 int paraht_reduce_d(paraht_ctx ctx, int n, double* A, int lda, double* B, int ldb, double* Q, int ldq, double* Z,
                     int ldz, int r, int p, int nq, int flags);
+
+/* ---- stage 2 without any allocation.  No counterpart in the reference.
+ * Same arithmetic and results as paraht_rht2ht_d (FP64 only), but the scratch (reflector
+ * stores, progress words) lives in a fixed file-scope device array of
+ * PARAHT_NOALLOC_SCRATCH_BYTES bytes instead of the context's workspace, so the call performs
+ * no cudaMalloc/cudaFree.  Returns PARAHT_ERR_TOO_LARGE if (n, r, nq) need more scratch than
+ * that (about n <= 4000 for r = nq = 16), PARAHT_ERR_NOT_SUPPORTED for PARAHT_FLAG_SPLIT or
+ * PARAHT_FLAG_TIME_COMPONENTS.  The scratch is shared by all callers on a device: calls that
+ * overlap in time (other threads, other contexts on the same device) race.  The first call on a
+ * device resolves the array's address (cudaGetSymbolAddress) and should precede any stream
+ * capture.  Everything that must start at zero is cleared on the stream by the call itself. ---- */
+#define PARAHT_NOALLOC_SCRATCH_BYTES (8u << 20)
+int paraht_rht2ht_d_noalloc(paraht_ctx ctx, int n, double* A, int lda, double* B, int ldb, double* Q, int ldq,
+                            double* Z, int ldz, int r, int nq, int flags);
 
 /* ---- batched: `count` independent pencils of possibly different sizes (device pointers).
  * Arrays of length count; r, p, nq per pencil.  No counterpart in the reference (it reduces one

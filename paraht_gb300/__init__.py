@@ -102,6 +102,12 @@ class Context:
         check(lib().paraht_rht2ht_d(self._h, int(n), A, int(lda), B, int(ldb), Q, int(ldq), Z, int(ldz), int(r),
                                     int(nq), int(flags)), "rht2ht_d")
 
+    def rht2ht_d_noalloc(self, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, nq, flags=0):
+        """paraht_rht2ht_d with the scratch in a fixed device array (no allocation; calls that
+        overlap in time on one device race)."""
+        check(lib().paraht_rht2ht_d_noalloc(self._h, int(n), A, int(lda), B, int(ldb), Q, int(ldq), Z, int(ldz),
+                                            int(r), int(nq), int(flags)), "rht2ht_d_noalloc")
+
     # -- host arrays on this context --
     def reduce_host(self, A, B, Q, Z, r, p, nq, flags=0):
         n = A.shape[0]

@@ -24,6 +24,7 @@ ERRORS = {
     -1005: "PARAHT_ERR_NOT_SUPPORTED",
     -1006: "PARAHT_ERR_NO_DEVICE",
     -1007: "PARAHT_ERR_BAD_CTX",
+    -1008: "PARAHT_ERR_TOO_LARGE",
 }
 
 # (name, argtypes) for every exported entry point; the tests check this list against the header.
@@ -43,6 +44,7 @@ SIGNATURES = {
     "paraht_ab2rht_d": [C.c_void_p, _i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i, _i],
     "paraht_rht2ht_d": [C.c_void_p, _i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i, _i],
     "paraht_reduce_d": [C.c_void_p, _i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i, _i, _i],
+    "paraht_rht2ht_d_noalloc": [C.c_void_p, _i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i, _i],
     "paraht_reduce_batched_d": [C.c_void_p, _i, C.POINTER(_i), C.POINTER(_d), C.POINTER(_i), C.POINTER(_d),
                                 C.POINTER(_i), C.POINTER(_d), C.POINTER(_i), C.POINTER(_d), C.POINTER(_i),
                                 C.POINTER(_i), C.POINTER(_i), C.POINTER(_i), _i],

@@ -4,6 +4,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
 #include <new>
 
 #include "launch_count.h"
@@ -24,6 +25,7 @@ static const uint32_t kMagic = 0x50485431u;  // "PHT1"
 namespace pht {
 
 void* Ctx::workspace(size_t bytes) {
+  if (ws_fixed) return bytes <= ws_fixed_bytes ? ws_fixed : nullptr;
   if (bytes <= ws_bytes) return ws;
   if (ws) {
     cudaStreamSynchronize(stream);
@@ -361,6 +363,49 @@ extern "C" int paraht_reduce_d(paraht_ctx c, int n, double* A, int lda, double* 
   return device_entry(c, 3, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, p, nq, flags);
 }
 
+// ---- stage 2 without allocation: the workspace is a fixed file-scope device array ----
+static __device__ __align__(256) unsigned char g_noalloc_scratch[PARAHT_NOALLOC_SCRATCH_BYTES];
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_addr[64];  // per device, resolved once
+
+extern "C" int paraht_rht2ht_d_noalloc(paraht_ctx c, int n, double* A, int lda, double* B, int ldb, double* Q,
+                                       int ldq, double* Z, int ldz, int r, int nq, int flags) {
+  if (!ctx_ok(c)) return PARAHT_ERR_BAD_CTX;
+  Ctx& x = c->c;
+  int rc = check_args(2, 1, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, 2, nq);
+  if (rc) return rc;
+  if (flags & (PARAHT_FLAG_SPLIT | PARAHT_FLAG_TIME_COMPONENTS)) return PARAHT_ERR_NOT_SUPPORTED;
+  if (pht::s2_workspace_bytes(n, r, nq) > (size_t)PARAHT_NOALLOC_SCRATCH_BYTES) return PARAHT_ERR_TOO_LARGE;
+  if (x.device < 0 || x.device >= 64) return PARAHT_ERR_NO_DEVICE;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(x.device);
+  void* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[x.device]) {
+      void* a = nullptr;
+      if (cudaGetSymbolAddress(&a, g_noalloc_scratch) != cudaSuccess || !a) {
+        cudaGetLastError();
+        cudaSetDevice(prev);
+        return PARAHT_ERR_CUDA;
+      }
+      g_noalloc_addr[x.device] = a;
+    }
+    scratch = g_noalloc_addr[x.device];
+  }
+  for (double& v : x.phase) v = 0.0;
+  x.residue[0] = x.residue[1] = 0.0;
+  x.ws_fixed = scratch;
+  x.ws_fixed_bytes = PARAHT_NOALLOC_SCRATCH_BYTES;
+  rc = run_device(x, 2, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, 2, nq, flags);
+  if (!rc) rc = finish(x);
+  x.ws_fixed = nullptr;
+  x.ws_fixed_bytes = 0;
+  cudaSetDevice(prev);
+  return rc;
+}
+
 // Host-pointer path: stage the four matrices into the context's device buffers, reduce, copy
 // back.  `off` is the argument-index offset (0 for context-free entry points).
 static int host_entry(paraht_ctx c, int off, int which, int n, double* A, int lda, double* B, int ldb, double* Q,
@@ -501,6 +546,8 @@ extern "C" const char* paraht_strerror(int s) {
       return "device-side wait timed out";
     case PARAHT_ERR_NONFINITE:
       return "non-finite input";
+    case PARAHT_ERR_TOO_LARGE:
+      return "problem needs more scratch than the fixed array of paraht_rht2ht_d_noalloc";
     case PARAHT_ERR_NOT_SUPPORTED:
       return "not supported";
     case PARAHT_ERR_NO_DEVICE:

@@ -52,6 +52,8 @@ struct Ctx {
   int num_sms = 0;
   void* ws = nullptr;  // workspace (grown on demand, reused across calls)
   size_t ws_bytes = 0;
+  void* ws_fixed = nullptr;  // when set, workspace() hands out this fixed region instead
+  size_t ws_fixed_bytes = 0;
   double* stage[4] = {nullptr, nullptr, nullptr, nullptr};  // device copies for host entries
   size_t stage_bytes = 0;
   cudaStream_t side = nullptr;      // second stream for work that overlaps the critical path
