@@ -20,6 +20,10 @@
 
 namespace pht {
 
+static inline __host__ __device__ int s1_round16(int x) { return (x + 15) / 16 * 16; }
+static inline __host__ __device__ int s1_lgen_pitch(int L) { return s1_round16(L) + 8; }
+static inline __host__ __device__ int s1_rgen_pitch(int L) { return s1_round16(L) + 4; }
+
 // Reflector scalars of DLARFG from alpha and the squared norm of x (see make_reflector).
 // tau, scal = 1/(alpha-beta), beta.
 PHT_DEV Reflector reflector_from_norm2(double alpha, double xnorm2) { return make_reflector(alpha, xnorm2); }
@@ -83,7 +87,9 @@ __global__ void __launch_bounds__(512) k_s1_lgen(double* __restrict__ A, int lda
                                                   double* __restrict__ TL) {
   extern __shared__ double sm[];
   constexpr int G = 8;
-  const int L = P.L, nb = P.nb, ldp = L + 1;
+  // column pitch = 8 (mod 16) doubles: the two columns a half-warp touches (8 lanes each, rows
+  // g = 0..7) fall into different banks
+  const int L = P.L, nb = P.nb, ldp = s1_lgen_pitch(L);
   double* Pt = sm;                    // ldp * nb
   double* G2 = Pt + (size_t)ldp * nb;  // nb*nb Gram
   double* Ts = G2 + nb * nb;          // nb*nb
@@ -175,14 +181,18 @@ __global__ void __launch_bounds__(512) k_s1_lgen(double* __restrict__ A, int lda
 // Ts (nb*nb), sc (4).
 // ------------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(512) k_s1_rgen(const double* __restrict__ B, int ldb, S1Panel P, int o,
-                                                  double* __restrict__ VRc, double* __restrict__ TR) {
+                                                  double* __restrict__ VRc, double* __restrict__ TR, int use_vr) {
   extern __shared__ double sm[];
   constexpr int Q = 4;
-  const int L = P.L, nb = P.nb, lds = L + 1;
+  // S column pitch = 4 (mod 16) doubles: a half-warp (4 rows x 4 column classes) hits 16
+  // distinct banks.  M (nb x L) is row-major, its rows read along the columns by 2..32 lanes.
+  // Vr (optional): the RQ reflectors row-major, read along columns while forming M.
+  const int L = P.L, nb = P.nb, lds = s1_rgen_pitch(L), ldm = lds;
   const int ib0 = P.ib(o), nb2 = P.nb2(o);
   double* S = sm;                       // lds * L
-  double* M = S + (size_t)lds * L;      // nb * L
-  double* dvec = M + (size_t)nb * L;    // L
+  double* M = S + (size_t)lds * L;      // nb * ldm
+  double* Vr = M + (size_t)nb * ldm;    // L * L when use_vr
+  double* dvec = Vr + (use_vr ? (size_t)L * L : 0);  // L
   double* tauR = dvec + L;              // L
   double* tauL = tauR + L;              // nb
   double* G2 = tauL + nb;               // nb*nb
@@ -240,34 +250,46 @@ __global__ void __launch_bounds__(512) k_s1_rgen(const double* __restrict__ B, i
     int QM = 1;  // lanes per row: largest power of two <= min(32, blockDim / nb)
     while (2 * QM <= 32 && 2 * QM * nb <= (int)blockDim.x) QM *= 2;
     const int r = t / QM, part = t % QM;
-    for (int e = t; e < nb * nb2; e += blockDim.x) M[(e % nb) + (e / nb) * nb] = ((e % nb) == (e / nb)) ? 1.0 : 0.0;
+    for (int e = t; e < nb * nb2; e += blockDim.x) M[(e / nb2) * ldm + e % nb2] = ((e / nb2) == (e % nb2)) ? 1.0 : 0.0;
+    if (use_vr)  // reflector of row i: S[i][0..i-1], implicit 1 at column i
+      for (int e = t; e < nb2 * nb2; e += blockDim.x) {
+        const int i = e / nb2, cc = e % nb2;
+        Vr[i * L + cc] = cc < i ? S[i + cc * lds] : 0.0;
+      }
     __syncthreads();
+    // rows of M are independent: each lane group runs through all reflectors without barriers
     for (int i = 0; i < nb2; ++i) {
       const double ti = tauR[i];
       if (ti == 0.0) continue;
       double s = 0.0;
       if (r < nb) {
-        for (int cc = part; cc < i; cc += QM) s = fma(M[r + cc * nb], S[i + cc * lds], s);
-        if (part == 0) s += M[r + i * nb];
+        if (use_vr)
+          for (int cc = part; cc < i; cc += QM) s = fma(M[r * ldm + cc], Vr[i * L + cc], s);
+        else
+          for (int cc = part; cc < i; cc += QM) s = fma(M[r * ldm + cc], S[i + cc * lds], s);
+        if (part == 0) s += M[r * ldm + i];
       }
       // reduce over the QM lanes of this row (QM divides 32)
       for (int off = 1; off < QM; off <<= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
       if (r < nb) {
         const double tw = ti * s;
-        for (int cc = part; cc < i; cc += QM) M[r + cc * nb] = fma(-tw, S[i + cc * lds], M[r + cc * nb]);
-        if (part == 0) M[r + i * nb] -= tw;
+        if (use_vr)
+          for (int cc = part; cc < i; cc += QM) M[r * ldm + cc] = fma(-tw, Vr[i * L + cc], M[r * ldm + cc]);
+        else
+          for (int cc = part; cc < i; cc += QM) M[r * ldm + cc] = fma(-tw, S[i + cc * lds], M[r * ldm + cc]);
+        if (part == 0) M[r * ldm + i] -= tw;
       }
-      __syncthreads();
     }
+    __syncthreads();
     // ---- LQ (dgelq2) of M: reflector i from row i, columns i..nb2-1; same lane layout ----
     for (int i = 0; i < nb; ++i) {
       double s = 0.0;
       if (r >= i && r < nb)
-        for (int cc = i + 1 + part; cc < nb2; cc += QM) s = fma(M[r + cc * nb], M[i + cc * nb], s);
+        for (int cc = i + 1 + part; cc < nb2; cc += QM) s = fma(M[r * ldm + cc], M[i * ldm + cc], s);
       for (int off = 1; off < QM; off <<= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
       if (r == i && part == 0) {
         dvec[r] = s;
-        const Reflector h = reflector_from_norm2(M[i + i * nb], s);
+        const Reflector h = reflector_from_norm2(M[i * ldm + i], s);
         sc[0] = h.tau;
         sc[1] = h.scal;
         sc[2] = h.beta;
@@ -277,16 +299,16 @@ __global__ void __launch_bounds__(512) k_s1_rgen(const double* __restrict__ B, i
       __syncthreads();
       const double tl = sc[0], scal = sc[1], beta = sc[2];
       if (r > i && r < nb && tl != 0.0) {
-        const double w = M[r + i * nb] + scal * dvec[r];
+        const double w = M[r * ldm + i] + scal * dvec[r];
         const double tw = tl * w, tws = tw * scal;
-        for (int cc = i + 1 + part; cc < nb2; cc += QM) M[r + cc * nb] = fma(-tws, M[i + cc * nb], M[r + cc * nb]);
-        if (part == 0) M[r + i * nb] -= tw;
+        for (int cc = i + 1 + part; cc < nb2; cc += QM) M[r * ldm + cc] = fma(-tws, M[i * ldm + cc], M[r * ldm + cc]);
+        if (part == 0) M[r * ldm + i] -= tw;
       }
       __syncthreads();
       if (r == i) {
-        for (int cc = i + 1 + part; cc < nb2; cc += QM) M[i + cc * nb] *= scal;
+        for (int cc = i + 1 + part; cc < nb2; cc += QM) M[i * ldm + cc] *= scal;
         if (part == 0) {
-          M[i + i * nb] = beta;
+          M[i * ldm + i] = beta;
           tauL[i] = tl;
         }
       }
@@ -296,7 +318,7 @@ __global__ void __launch_bounds__(512) k_s1_rgen(const double* __restrict__ B, i
     for (int e = t; e < L * nb; e += blockDim.x) {
       const int cc = e % L, i = e / L;
       double v = 0.0;
-      if (cc < nb2) v = (cc < i) ? 0.0 : (cc == i ? 1.0 : M[i + cc * nb]);
+      if (cc < nb2) v = (cc < i) ? 0.0 : (cc == i ? 1.0 : M[i * ldm + cc]);
       V[cc + (size_t)i * L] = v;
     }
     // Gram G2[a][b] = VR[a] . VR[b] (a < b)
@@ -307,9 +329,9 @@ __global__ void __launch_bounds__(512) k_s1_rgen(const double* __restrict__ B, i
         const int a = e % nb, b = e / nb;
         double s = 0.0;
         if (e < nb * nb && a < b)
-          for (int cc = b + 1 + part; cc < nb2; cc += QM) s = fma(M[a + cc * nb], M[b + cc * nb], s);
+          for (int cc = b + 1 + part; cc < nb2; cc += QM) s = fma(M[a * ldm + cc], M[b * ldm + cc], s);
         for (int off = 1; off < QM; off <<= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-        if (part == 0 && e < nb * nb) G2[a + b * nb] = (a < b) ? s + M[a + b * nb] : 0.0;
+        if (part == 0 && e < nb * nb) G2[a + b * nb] = (a < b) ? s + M[a * ldm + b] : 0.0;
       }
     }
     __syncthreads();
@@ -337,10 +359,14 @@ __global__ void __launch_bounds__(512) k_s1_rgen(const double* __restrict__ B, i
   }
 }
 
-size_t s1_lgen_smem(int L, int nb) { return sizeof(double) * ((size_t)(L + 1) * nb + 2 * nb * nb + 2 * nb + 4); }
-size_t s1_rgen_smem(int L, int nb) {
-  return sizeof(double) * ((size_t)(L + 1) * L + (size_t)nb * L + 2 * (size_t)L + nb + 2 * nb * nb + 4);
+size_t s1_lgen_smem(int L, int nb) {
+  return sizeof(double) * ((size_t)s1_lgen_pitch(L) * nb + 2 * nb * nb + 2 * nb + 4);
 }
+static size_t s1_rgen_smem_vr(int L, int nb, bool vr) {
+  const size_t p = (size_t)s1_rgen_pitch(L);
+  return sizeof(double) * (p * L + (size_t)nb * p + (vr ? (size_t)L * L : 0) + 2 * (size_t)L + nb + 2 * nb * nb + 4);
+}
+size_t s1_rgen_smem(int L, int nb) { return s1_rgen_smem_vr(L, nb, false); }
 int s1_rgen_threads(int L) { return 4 * (((L + 7) / 8) * 8); }  // 4 lanes per row, multiple of 32
 int s1_lgen_threads(int nb) { return ((8 * nb + 31) / 32) * 32; }  // 8 lanes per column
 
@@ -360,8 +386,15 @@ void launch_s1_rgen(cudaStream_t s, const double* B, int ldb, const S1Panel& P, 
     cudaFuncSetAttribute(k_s1_rgen, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     attr = true;
   }
+  static int max_smem = -1;
+  if (max_smem < 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  }
+  const bool vr = s1_rgen_smem_vr(P.L, P.nb, true) <= (size_t)max_smem;
   count_launch();
-  k_s1_rgen<<<1, s1_rgen_threads(P.L), s1_rgen_smem(P.L, P.nb), s>>>(B, ldb, P, o, VRc, TR);
+  k_s1_rgen<<<1, s1_rgen_threads(P.L), s1_rgen_smem_vr(P.L, P.nb, vr), s>>>(B, ldb, P, o, VRc, TR, vr ? 1 : 0);
 }
 
 }  // namespace pht

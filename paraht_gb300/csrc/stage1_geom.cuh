@@ -38,6 +38,11 @@ struct GeoS1Left {
   PHT_DEV int count() const { return P.nblocks; }
   PHT_DEV int slot_op(int s) const { return s; }
   PHT_DEV int op_slot(int o) const { return o; }
+  PHT_DEV bool masks_y() const { return false; }
+  PHT_DEV void range(int, const WYOp& w, int, int& a, int& b) const {
+    a = 0;
+    b = w.k - 1;
+  }
   PHT_DEV WYOp op(int o) const {
     WYOp w;
     w.start = P.ib(o);
@@ -61,6 +66,11 @@ struct GeoS1Q {
   PHT_DEV int count() const { return P.nblocks; }
   PHT_DEV int slot_op(int s) const { return s; }
   PHT_DEV int op_slot(int o) const { return o; }
+  PHT_DEV bool masks_y() const { return false; }
+  PHT_DEV void range(int, const WYOp& w, int, int& a, int& b) const {
+    a = 0;
+    b = w.k - 1;
+  }
   PHT_DEV WYOp op(int o) const {
     WYOp w;
     w.start = P.ib(o);
@@ -87,6 +97,11 @@ struct GeoS1Right {
   PHT_DEV int count() const { return bl_only >= 0 ? 1 : P.nblocks; }
   PHT_DEV int slot_op(int s) const { return s; }
   PHT_DEV int op_slot(int o) const { return o; }
+  PHT_DEV bool masks_y() const { return false; }
+  PHT_DEV void range(int, const WYOp& w, int, int& a, int& b) const {
+    a = 0;
+    b = w.k - 1;
+  }
   PHT_DEV WYOp op(int i) const {
     const int o = bl_only >= 0 ? bl_only : i;
     WYOp w;

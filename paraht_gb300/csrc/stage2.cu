@@ -36,19 +36,50 @@ enum S2Kind {
 struct GeoS2 {
   S2Store S;
   int n, J, r, nq, nblocks, kind;  // J = jblock (1-based)
-  PHT_DEV int count() const {
-    switch (kind) {
-      case kLaRight:
-      case kUpRight:
-        return nblocks * nq;
-      default:
-        return nblocks;
+  // blk = 1: one op per block also for kLaRight / kUpRight, whose single reflectors act on a
+  // staircase of rows; range() gives each row its contiguous subset of the block's reflectors
+  // (the split-precision kernel, wy_stream.cuh).  blk = 0: the reference's op sequence with
+  // the single reflectors as separate ops (FP64 kernels).
+  int blk = 0;
+  PHT_DEV bool per_refl() const { return !blk && (kind == kLaRight || kind == kUpRight); }
+  PHT_DEV int count() const { return per_refl() ? nblocks * nq : nblocks; }
+  PHT_DEV int slot_op(int s) const { return s; }
+  PHT_DEV int op_slot(int o) const { return o; }
+  // Whether some row stops before the block's last reflector (the lookahead staircase): the
+  // split kernel then forms Y = X T and masks it (wy_stream.cuh).
+  PHT_DEV bool masks_y() const { return blk && kind == kLaRight; }
+  // Reflectors [a, b] (0-based) of op o applied to strip row `row` (0-based, lo <= row <= hi).
+  PHT_DEV void range(int o, const WYOp& w, int row, int& a, int& b) const {
+    a = 0;
+    b = w.k - 1;
+    if (!blk || (kind != kUpRight && kind != kLaRight)) return;
+    const int ib = nblocks - o;
+    const int base = J + 1 + (ib - 1) * r;
+    const int R1 = row + 1, D = base - R1;  // 1-based row, distance to the block's first row
+    if (kind == kUpRight) {
+      // rows 1 .. istart-1: the whole block (rht2ht.f90:1894-1920); rows istart ..: the single
+      // reflectors ic = 2..nq with row < istart2(ic) = base - (2nq-ic) r (:1818-1844)
+      const int istart = max(J + 1, base - (2 * nq - 1) * r);
+      if (R1 <= istart - 1) return;
+      if (D < 1) {
+        a = 1;
+        b = 0;
+        return;
+      }
+      a = max(2, 2 * nq - (D - 1) / r) - 1;
+      return;
     }
+    // lookahead (:1644-1661, 1710-1728): reflector ic on rows [istart(ic), istart2(ic)),
+    // istart(ic) = max(J+1, base - (2nq-ic) r), istart2(ic) = max(J+1, base - (nq-ic) r)
+    if (R1 < J + 1 || D < 1) {
+      a = 1;
+      b = 0;
+      return;
+    }
+    const int cd = (D + r - 1) / r;
+    a = max(1, nq - cd + 1) - 1;
+    b = min(w.k, 2 * nq - cd) - 1;
   }
-  // Split-precision preparation slots: only the compact-WY ops (kUpRight: the last op of each
-  // block; single reflectors are applied in FP64 by the split kernel and need no slot).
-  PHT_DEV int slot_op(int s) const { return kind == kUpRight ? s * nq + nq - 1 : s; }
-  PHT_DEV int op_slot(int o) const { return kind == kUpRight ? o / nq : o; }
   PHT_DEV WYOp single(int ic, int ib, int rlo1, int rhi1) const {  // 1-based inclusive rows
     const int jb = J + (ib - 1) * r;
     WYOp w;
@@ -65,6 +96,25 @@ struct GeoS2 {
   }
   PHT_DEV WYOp op(int o) const {
     WYOp w;
+    if (blk && (kind == kLaRight || kind == kUpRight)) {  // the block's compact WY, row staircase
+      const int ib = nblocks - o;
+      const int jb = J + (ib - 1) * r, base = J + 1 + (ib - 1) * r;
+      w.start = jb;
+      w.len = min(n - jb, r + nq);
+      w.k = min(nq, w.len);
+      w.V = S.V + S.ui(1, 1, ib);
+      w.ldv = S.ldu;
+      w.T = S.TV + S.tt(ib);
+      w.ldt = nq;
+      if (kind == kUpRight) {
+        w.lo = 0;
+        w.hi = max(max(J + 1, base - (2 * nq - 1) * r) - 2, max(J + 1, base - nq * r) - 2);
+      } else {
+        w.lo = max(J + 1, base - (2 * nq - 1) * r) - 1;
+        w.hi = base - 2;
+      }
+      return w;
+    }
     if (kind == kLaRight || kind == kUpRight) {
       const int ib = nblocks - o / nq, sub = o % nq;
       const int base = J + 1 + (ib - 1) * r;
@@ -216,8 +266,10 @@ int s2_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
     cudaEventRecord(ctx.ev_a, sg);
     cudaStreamWaitEvent(su, ctx.ev_a, 0);
   }
-  // split-precision bulk updates where the op shapes fit (k = nq reflectors, r+nq long);
-  // regions: 0 B right, 1 A right, 2 B left, 3 A left, 4 Q, 5 Z
+  // split-precision lookahead and bulk updates where the op shapes fit (k = nq reflectors,
+  // r+nq long).  Operand regions (one per op list; lists applied to both A and B share one):
+  // 0 bulk right, 1 bulk left, 2 Q, 3 Z (side stream), 4 lookahead right, 5 lookahead left
+  // (main stream)
   const bool sp = ctx.split && split_fits(nq, r + nq);
   void* reg[6] = {};
   if (sp)
@@ -242,12 +294,13 @@ int s2_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
     if (timer) timer->mark(sg, 1);
     if (k > 0 && su != sg) cudaStreamWaitEvent(sg, ctx.ev_b, 0);  // lookahead k after bulk k-1
     GeoS2 g{St, n, J, r, nq, nblocks, kLaRight};
-    launch_apply_right(B, ldb, J, n - 1, g, sg);  // rows >= istart >= jblock+1
-    launch_apply_right(A, lda, J, n - 1, g, sg);
+    g.blk = sp ? 1 : 0;  // split kernel: one op per block, row staircase through range()
+    apply_right_any(reg[4], B, ldb, J, n - 1, g, nblocks, sg);  // rows >= istart >= jblock+1
+    apply_right_any(reg[4], A, lda, J, n - 1, g, nblocks, sg, false);
     g.kind = kLaLeftB;
-    launch_apply_left(B, ldb, J, n - 1, g, sg);
+    apply_left_any(reg[5], B, ldb, J, n - 1, g, nblocks, sg);
     g.kind = kLaLeftA;
-    launch_apply_left(A, lda, J, n - 1, g, sg);
+    apply_left_any(reg[5], A, lda, J, n - 1, g, nblocks, sg, false);
     if (timer) timer->mark(sg, 2);
     if (su != sg) {
       cudaEventRecord(ctx.ev_a, sg);
@@ -257,14 +310,14 @@ int s2_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
     // block ib-1's staircase range, so singles and blocks form one ordered list
     g.kind = kUpRight;
     apply_right_any(reg[0], B, ldb, 0, n - 1, g, nblocks, su);
-    apply_right_any(reg[1], A, lda, 0, n - 1, g, nblocks, su);
+    apply_right_any(reg[0], A, lda, 0, n - 1, g, nblocks, su, false);
     g.kind = kUpLeft;
-    apply_left_any(reg[2], B, ldb, J, n - 1, g, nblocks, su);
-    apply_left_any(reg[3], A, lda, J, n - 1, g, nblocks, su);
+    apply_left_any(reg[1], B, ldb, J, n - 1, g, nblocks, su);
+    apply_left_any(reg[1], A, lda, J, n - 1, g, nblocks, su, false);
     g.kind = kUpQ;
-    apply_right_any(reg[4], Q, ldq, 0, n - 1, g, nblocks, su);
+    apply_right_any(reg[2], Q, ldq, 0, n - 1, g, nblocks, su);
     g.kind = kUpZ;
-    apply_right_any(reg[5], Z, ldz, 0, n - 1, g, nblocks, su);
+    apply_right_any(reg[3], Z, ldz, 0, n - 1, g, nblocks, su);
     if (su != sg) cudaEventRecord(ctx.ev_b, su);
   }
   if (su != sg) cudaStreamWaitEvent(sg, ctx.ev_b, 0);
