@@ -47,14 +47,15 @@ def parse():
     ap.add_argument("--impl", choices=("paraht", "reference"), default="paraht")
     ap.add_argument("--n", type=int, default=16000)
     ap.add_argument("--r", type=int, default=16)
-    ap.add_argument("--p", type=int, default=2)
+    ap.add_argument("--p", type=int, default=4)
     ap.add_argument("--nq", type=int, default=16)
     ap.add_argument("--dist", default="std")
-    ap.add_argument("--precision", choices=("fp64", "split"), default="fp64")
+    ap.add_argument("--precision", choices=("fp64", "split"), default="split")
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--cpu-sample-n", type=int, default=2500)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--check", action="store_true", help="also compute the backward error of the last step")
+    ap.add_argument("--phases", action="store_true", help="one extra serialised step for the per-phase times")
     return ap.parse_args()
 
 
@@ -198,12 +199,34 @@ def main():
         ctx.reduce_d(n, work[0].data_ptr(), n, work[1].data_ptr(), n, work[2].data_ptr(), n, work[3].data_ptr(), n,
                      r, p, nq, f)
 
-    for _ in range(args.warmup):
-        restore()
-        step()
+    # host-pointer entry point (the reference-facing call): pinned host buffers, copies inside
+    hostA = torch.from_numpy(np.asfortranarray(A0).T.copy()).pin_memory()
+    hostB = torch.from_numpy(np.asfortranarray(B0).T.copy()).pin_memory()
+    hostQ = torch.empty((n, n), dtype=torch.float64).pin_memory()
+    hostZ = torch.empty((n, n), dtype=torch.float64).pin_memory()
+
+    def host_step():
+        hostA.copy_(torch.from_numpy(np.asfortranarray(A0).T))
+        hostB.copy_(torch.from_numpy(np.asfortranarray(B0).T))
+        hostQ.copy_(torch.eye(n, dtype=torch.float64))
+        hostZ.copy_(torch.eye(n, dtype=torch.float64))
+        nA, nB, nQ, nZ = (x.numpy().T for x in (hostA, hostB, hostQ, hostZ))  # Fortran-ordered views
+        barrier()
+        t0 = time.perf_counter()
+        ctx.reduce_host(nA, nB, nQ, nZ, r, p, nq, flags)
+        return time.perf_counter() - t0
+
+    # warm-up: the last one goes through the host entry point (sizes its staging buffers)
+    for i in range(args.warmup):
+        if i == args.warmup - 1:
+            host_step()
+        else:
+            restore()
+            step()
     torch.cuda.synchronize()
     ms = []
     launches = 0
+    kst = {"stage1": {"seconds": 0.0, "launches": 0, "flops": 0.0}, "stage2": {"seconds": 0.0, "launches": 0, "flops": 0.0}}
     sampler = ClockSampler(local)
     with sampler:
         for _ in range(args.steps):
@@ -212,11 +235,15 @@ def main():
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            step()
+            step(flags | ph.PARAHT_FLAG_KERNEL_TIMES)
             e1.record(stream)
             e1.synchronize()
             ms.append(e0.elapsed_time(e1))
             launches += ctx.launch_count()
+            st = ctx.kernel_stats()
+            for k in kst:
+                for f in kst[k]:
+                    kst[k][f] += st[k][f]
             barrier()
     t_step = statistics.mean(ms) / 1e3
     if dist_on:
@@ -230,62 +257,46 @@ def main():
     # backward error of the last timed step (outside the timed region)
     check = None
     if args.check:
-        Qd, Zd = work[2], work[3]
-        A0d = dev0[0]
-        # column-major data stored as row-major transposes: X^T tensors -> use .T views
-        H, T, Q, Z = work[0].T, work[1].T, Qd.T, Zd.T
-        Af, Bf = A0d.T, dev0[1].T
+        H, T, Q, Z = work[0].T, work[1].T, work[2].T, work[3].T
+        Af, Bf = dev0[0].T, dev0[1].T  # column-major data stored as row-major transposes
         ea = float(torch.linalg.norm(Q.T @ Af @ Z - H) / torch.linalg.norm(Af))
         eb = float(torch.linalg.norm(Q.T @ Bf @ Z - T) / torch.linalg.norm(Bf))
         check = {"bwd_err_A": ea, "bwd_err_B": eb, "bound_10n_eps": 10 * n * EPS}
 
-    # one instrumented step for the phase breakdown (time_components serialises the streams)
-    restore()
-    step(flags | ph.PARAHT_FLAG_TIME_COMPONENTS)
-    phases = ctx.phase_times()
+    # end to end through the host entry point, copies inside the timed region
+    e2e_v = statistics.mean([host_step() for _ in range(max(1, args.e2e_steps))]) / world
 
-    # end to end through the public host entry point (pinned host buffers, copies timed)
-    hostA = torch.from_numpy(np.asfortranarray(A0).T.copy()).pin_memory()
-    hostB = torch.from_numpy(np.asfortranarray(B0).T.copy()).pin_memory()
-    hostQ = torch.empty((n, n), dtype=torch.float64).pin_memory()
-    hostZ = torch.empty((n, n), dtype=torch.float64).pin_memory()
-    e2e_t = []
-    for i in range(args.e2e_steps + 1):
-        hostA.copy_(torch.from_numpy(np.asfortranarray(A0).T))
-        hostB.copy_(torch.from_numpy(np.asfortranarray(B0).T))
-        hostQ.copy_(torch.eye(n, dtype=torch.float64))
-        hostZ.copy_(torch.eye(n, dtype=torch.float64))
-        nA, nB, nQ, nZ = (x.numpy().T for x in (hostA, hostB, hostQ, hostZ))  # Fortran-ordered views
-        barrier()
-        t0 = time.perf_counter()
-        ctx.reduce_host(nA, nB, nQ, nZ, r, p, nq, flags)
-        dt = time.perf_counter() - t0
-        if i > 0 or args.e2e_steps == 0:  # first call sizes the staging buffers
-            e2e_t.append(dt)
-    e2e_v = statistics.mean(e2e_t) / world
+    phases = None
+    if args.phases:  # time_components serialises the streams: one extra, slower step
+        restore()
+        step(flags | ph.PARAHT_FLAG_TIME_COMPONENTS)
+        phases = {k: round(v, 4) for k, v in ctx.phase_times().items()}
 
-    # roofline of the dominant phase (stage-1 and stage-2 bulk updates run on FP64 CUDA cores)
+    # roofline of the dominant kernel: the compact-WY op-list kernel of stage 2 (bulk and
+    # lookahead updates), timed launch by launch with CUDA events on its streams during the timed
+    # steps; its algorithmic work is 4 len k FP64-equivalent flops per strip row per op
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
         pass
-    f1 = 4.0 * p / (p - 1) * (7.0 / 3.0) * n ** 3  # stage-1 useful flops
-    f2 = 8.0 * n ** 3                                 # stage-2 useful flops
-    t1 = phases["s1_genleft"] + phases["s1_genright"] + phases["s1_mul"]
-    t2 = phases["s2_gen"] + phases["s2_lookahead"] + phases["s2_application"]
-    fp64_peak = 1.19  # TFLOP/s, FP64 FMA throughput measured on this GB300 (not in MEASURED_PEAKS.json)
-    mul_t = phases["s1_mul"] + phases["s2_application"]
-    mul_f = f1 + f2
-    achieved = mul_f / mul_t / 1e12 if mul_t > 0 else None
-    roofline = {
-        "bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-        "frac": (achieved / fp64_peak) if achieved else None, "traffic": None,
-        "kernel": "k_apply_left/k_apply_right (compact-WY bulk updates, FP64 CUDA cores)",
-        "peak_source": "FP64 FMA throughput measured on this pool's GB300 (1.19 TFLOP/s); MEASURED_PEAKS.json "
-                       f"lists HBM {peaks.get('hbm_gbs')} GB/s and bf16 {peaks.get('bf16_tflops')} TFLOP/s only",
-        "stage_seconds": {"stage1": t1, "stage2": t2},
-    }
+    s2 = kst["stage2"]
+    if args.precision == "split":
+        # each FP64-equivalent flop is 36 FP16 digit-pair flops on the tensor cores
+        peak = float(peaks.get("bf16_tflops", 1900.0))
+        achieved = 36.0 * s2["flops"] / s2["seconds"] / 1e12 if s2["seconds"] > 0 else None
+        roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                    "frac": achieved / peak if achieved else None, "traffic": None,
+                    "kernel": "k_ws_apply<GeoS2> (split-precision compact-WY op lists, FP16 digit MMAs)",
+                    "peak_source": "MEASURED_PEAKS.json bf16_tflops (FP16 and BF16 mma run at the same rate), of measured",
+                    "fp64_equivalent_tflops": s2["flops"] / s2["seconds"] / 1e12 if s2["seconds"] > 0 else None,
+                    "launches_per_step": s2["launches"] / max(1, args.steps),
+                    "avg_launch_ms": 1e3 * s2["seconds"] / max(1, s2["launches"])}
+    else:
+        fp64_peak = 1.19  # TFLOP/s, FP64 FMA throughput measured on this machine's GB300
+        roofline = {"bound": "fp64", "achieved": None, "peak": fp64_peak, "unit": "TFLOP/s", "frac": None,
+                    "traffic": None, "kernel": "k_apply_left/k_apply_right (FP64 compact-WY op lists)",
+                    "peak_source": "FP64 FMA throughput measured on this pool's GB300 (fp64 probe)"}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -308,7 +319,6 @@ def main():
                        "l2": "inputs 8.2 GB >> L2; pristine input restored between steps outside the timed region"},
             "e2e": {"value": e2e_v, "unit": "s", "h2d_bytes_per_step": 4 * n * n * 8, "d2h_bytes_per_step": 4 * n * n * 8},
             "gpu_launches": launches,
-            "phases_s": {k: round(v, 4) for k, v in phases.items()},
             "effective_gflops": flops_nominal(n) / t_step / 1e9,
             "roofline": roofline,
             "cpu_baseline": cpu,
@@ -316,6 +326,8 @@ def main():
         }
         if check:
             line["check"] = check
+        if phases:
+            line["phases_s"] = phases
         print(json.dumps(line), flush=True)
     if dist_on:
         import torch.distributed as td

@@ -54,6 +54,8 @@ extern "C" {
 #define PARAHT_FLAG_SEQUENTIAL 16     /* debug: run the stage-2 sweeps of a group one after the other in
                                          one CTA and all updates on one stream (the reference's order);
                                          results are bitwise identical to the default pipelined schedule */
+#define PARAHT_FLAG_KERNEL_TIMES 32   /* time every split-precision op-list launch with CUDA events and
+                                         count its algorithmic work (paraht_ctx_kernel_stats) */
 
 typedef struct paraht_ctx_s* paraht_ctx;
 
@@ -73,6 +75,11 @@ int paraht_ctx_launch_count(paraht_ctx ctx, long long* count);
 /* Largest absolute entry found below the structure (r-Hessenberg / Hessenberg for A,
  * triangular for B) before it was zeroed by the last call: [0] A, [1] B. */
 int paraht_ctx_fill_residue(paraht_ctx ctx, double* residue, int nres);
+/* With PARAHT_FLAG_KERNEL_TIMES, for the split-precision compact-WY op-list kernel of the last
+ * call: [0] summed launch durations (s), [1] launches, [2] algorithmic FP64-equivalent flops
+ * (4 len k per strip row per op) of the stage-1 lists; [3..5] the same for the stage-2 lists.
+ * No counterpart in the reference. */
+int paraht_ctx_kernel_stats(paraht_ctx ctx, double* stats, int nstats);
 
 /* ---- host-pointer drop-ins (copy in, reduce on the GPU, copy out) ----
  * paraht_ab2rht  <-> ab2rht_simple(n, A, lda, B, ldb, Q, ldq, Z, ldz, nb, p, time_components)

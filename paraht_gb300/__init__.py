@@ -22,13 +22,13 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import (PARAHT_FLAG_CHECK_FINITE, PARAHT_FLAG_NO_ZERO_FILL, PARAHT_FLAG_SEQUENTIAL, PARAHT_FLAG_SPLIT,
-                   PARAHT_FLAG_TIME_COMPONENTS, ParahtError, check, lib)
+from ._lib import (PARAHT_FLAG_CHECK_FINITE, PARAHT_FLAG_KERNEL_TIMES, PARAHT_FLAG_NO_ZERO_FILL,
+                   PARAHT_FLAG_SEQUENTIAL, PARAHT_FLAG_SPLIT, PARAHT_FLAG_TIME_COMPONENTS, ParahtError, check, lib)
 
 __all__ = [
     "ab2rht_simple", "rht2ht_householder", "reduce", "Context", "ParahtError",
     "PARAHT_FLAG_TIME_COMPONENTS", "PARAHT_FLAG_CHECK_FINITE", "PARAHT_FLAG_SPLIT", "PARAHT_FLAG_NO_ZERO_FILL",
-    "PARAHT_FLAG_SEQUENTIAL",
+    "PARAHT_FLAG_SEQUENTIAL", "PARAHT_FLAG_KERNEL_TIMES",
 ]
 
 PHASE_NAMES = ("s1_genleft", "s1_genright", "s1_mul", "s2_gen", "s2_lookahead", "s2_application", "copies", "total")
@@ -101,6 +101,15 @@ class Context:
     def rht2ht_d(self, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, nq, flags=0):
         check(lib().paraht_rht2ht_d(self._h, int(n), A, int(lda), B, int(ldb), Q, int(ldq), Z, int(ldz), int(r),
                                     int(nq), int(flags)), "rht2ht_d")
+
+    def kernel_stats(self):
+        """Split-precision op-list kernel statistics of the last call made with
+        PARAHT_FLAG_KERNEL_TIMES: per stage, summed launch seconds, launches and algorithmic
+        FP64-equivalent flops."""
+        out = (C.c_double * 6)()
+        check(lib().paraht_ctx_kernel_stats(self._h, out, 6), "kernel_stats")
+        return {"stage1": {"seconds": out[0], "launches": int(out[1]), "flops": out[2]},
+                "stage2": {"seconds": out[3], "launches": int(out[4]), "flops": out[5]}}
 
     def rht2ht_d_noalloc(self, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, nq, flags=0):
         """paraht_rht2ht_d with the scratch in a fixed device array (no allocation; calls that

@@ -15,6 +15,7 @@ PARAHT_FLAG_CHECK_FINITE = 2
 PARAHT_FLAG_SPLIT = 4
 PARAHT_FLAG_NO_ZERO_FILL = 8
 PARAHT_FLAG_SEQUENTIAL = 16
+PARAHT_FLAG_KERNEL_TIMES = 32
 
 ERRORS = {
     -1001: "PARAHT_ERR_CUDA",
@@ -44,6 +45,7 @@ SIGNATURES = {
     "paraht_ab2rht_d": [C.c_void_p, _i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i, _i],
     "paraht_rht2ht_d": [C.c_void_p, _i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i, _i],
     "paraht_reduce_d": [C.c_void_p, _i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i, _i, _i],
+    "paraht_ctx_kernel_stats": [C.c_void_p, C.POINTER(C.c_double), _i],
     "paraht_rht2ht_d_noalloc": [C.c_void_p, _i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i, _i],
     "paraht_reduce_batched_d": [C.c_void_p, _i, C.POINTER(_i), C.POINTER(_d), C.POINTER(_i), C.POINTER(_d),
                                 C.POINTER(_i), C.POINTER(_d), C.POINTER(_i), C.POINTER(_d), C.POINTER(_i),

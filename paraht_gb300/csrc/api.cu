@@ -14,6 +14,30 @@
 
 namespace pht {
 thread_local long long tl_launches = 0;
+thread_local KernelClock* tl_kclock = nullptr;
+
+// Next event pair for a timed launch; events are created on first use and kept by the context.
+bool KernelClock::pair(int st, cudaEvent_t* e0, cudaEvent_t* e1) {
+  auto* c = static_cast<Ctx::Clock*>(this);
+  constexpr size_t kMaxPairs = size_t(1) << 20;
+  if (c->used >= kMaxPairs) return false;
+  if (2 * c->used + 2 > c->ev.size()) {
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
+      cudaGetLastError();
+      if (a) cudaEventDestroy(a);
+      return false;
+    }
+    c->ev.push_back(a);
+    c->ev.push_back(b);
+    c->site.push_back(0);
+  }
+  *e0 = c->ev[2 * c->used];
+  *e1 = c->ev[2 * c->used + 1];
+  c->site[c->used] = st;
+  ++c->used;
+  return true;
+}
 }
 
 struct paraht_ctx_s {
@@ -192,6 +216,8 @@ extern "C" int paraht_ctx_destroy(paraht_ctx c) {
   }
   if (x.ev_a) cudaEventDestroy(x.ev_a);
   if (x.ev_b) cudaEventDestroy(x.ev_b);
+  for (auto e : x.kc.ev) cudaEventDestroy(e);
+  if (x.kc.dflops) cudaFree(x.kc.dflops);
   for (auto e : x.ev)
     if (e) cudaEventDestroy(e);
   cudaSetDevice(prev);
@@ -229,6 +255,13 @@ extern "C" int paraht_ctx_launch_count(paraht_ctx c, long long* count) {
   if (!ctx_ok(c)) return PARAHT_ERR_BAD_CTX;
   if (!count) return -2;
   *count = c->c.launches;
+  return 0;
+}
+
+extern "C" int paraht_ctx_kernel_stats(paraht_ctx c, double* st, int ns) {
+  if (!ctx_ok(c)) return PARAHT_ERR_BAD_CTX;
+  if (!st) return -2;
+  for (int i = 0; i < ns && i < 6; ++i) st[i] = c->c.kstats[i];
   return 0;
 }
 
@@ -284,6 +317,18 @@ static int run_device(Ctx& x, int which, int n, double* A, int lda, double* B, i
   }
   const long long launches0 = pht::tl_launches;
   const bool timed = flags & PARAHT_FLAG_TIME_COMPONENTS;
+  const bool ktimes = flags & PARAHT_FLAG_KERNEL_TIMES;
+  for (double& v : x.kstats) v = 0.0;
+  if (ktimes) {
+    if (!x.kc.dflops && cudaMalloc(&x.kc.dflops, 2 * sizeof(unsigned long long)) != cudaSuccess) {
+      cudaGetLastError();
+      x.kc.dflops = nullptr;
+      return PARAHT_ERR_ALLOC;
+    }
+    cudaMemsetAsync(x.kc.dflops, 0, 2 * sizeof(unsigned long long), x.stream);
+    x.kc.used = 0;
+    pht::tl_kclock = &x.kc;
+  }
   if (flags & PARAHT_FLAG_CHECK_FINITE) {
     const int rc = pht::check_finite(x.stream, n, A, lda, B, ldb, x.dstatus);
     if (rc) return rc;
@@ -329,6 +374,22 @@ static int run_device(Ctx& x, int which, int n, double* A, int lda, double* B, i
   }
   if (!rc) rc = finish(x);
   if (!rc && hstatus) rc = hstatus;
+  pht::tl_kclock = nullptr;
+  if (!rc && ktimes) {  // all streams have joined the main stream, which finish() synchronized
+    for (size_t i = 0; i < x.kc.used; ++i) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, x.kc.ev[2 * i], x.kc.ev[2 * i + 1]) != cudaSuccess) {
+        cudaGetLastError();
+        continue;
+      }
+      x.kstats[3 * x.kc.site[i]] += ms * 1e-3;
+      x.kstats[3 * x.kc.site[i] + 1] += 1.0;
+    }
+    unsigned long long fl[2] = {0, 0};
+    cudaMemcpy(fl, x.kc.dflops, sizeof(fl), cudaMemcpyDeviceToHost);
+    x.kstats[2] = (double)fl[0];
+    x.kstats[5] = (double)fl[1];
+  }
   x.launches = pht::tl_launches - launches0;
   return rc;
 }

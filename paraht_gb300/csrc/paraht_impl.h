@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "../../include/paraht.h"
+#include "launch_count.h"
 
 namespace pht {
 
@@ -76,6 +77,14 @@ struct Ctx {
   double* dresidue = nullptr;
   void* workspace(size_t bytes);
   int ensure_staging(size_t bytes_each);
+  // PARAHT_FLAG_KERNEL_TIMES: event pairs of the timed launches (reused across calls), their
+  // sites, and the statistics of the last call
+  struct Clock : KernelClock {
+    std::vector<cudaEvent_t> ev;
+    std::vector<int> site;
+    size_t used = 0;
+  } kc;
+  double kstats[6] = {0};
 };
 
 size_t s1_workspace_bytes(int n, int nb, int p);

@@ -460,9 +460,8 @@ int s1_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
       GeoS1Right gl{P, VRc[s], TR[s], o};
       gl.row_lo = c1;
       gl.row_hi = P.ib2(o);
-      // split precision: operand slot 0 of region 0 (the B left update above, on the same
-      // stream, has finished with it)
-      apply_right_any(reg[0], B, ldb, c1, P.ib2(o), gl, 1, sA);
+      // a small update on the critical chain: FP64, 8 rows per CTA
+      launch_apply_right<GeoS1Right, 8>(B, ldb, c1, P.ib2(o), gl, sA);
       if (P.nb2(o) > nb) {
         count_launch();
         k_s1_zero_fill<<<nb, 128, 0, sA>>>(B, ldb, P.ib(o), P.ib2(o), nb);

@@ -197,47 +197,98 @@ __global__ void __launch_bounds__(512) k_s1_rgen(const double* __restrict__ B, i
   double* tauL = tauR + L;              // nb
   double* G2 = tauL + nb;               // nb*nb
   double* Ts = G2 + nb * nb;            // nb*nb
-  double* sc = Ts + nb * nb;            // 4
-  const int t = threadIdx.x, rho = t / Q, q = t % Q;
+  double* sc = Ts + nb * nb;            // 4, then 2 (L+1) for the published RQ reflectors
+  const int t = threadIdx.x;
   for (int e = t; e < nb2 * nb2; e += blockDim.x) {
     const int i = e % nb2, j = e / nb2;
     S[i + j * lds] = B[(size_t)(ib0 + i) + (size_t)(ib0 + j) * ldb];
   }
   __syncthreads();
-  // ---- RQ (dgerq2): rows bottom to top; reflector of row i acts on columns 0..i ----
-  for (int i = nb2 - 1; i >= 0; --i) {
-    // d_rho = sum_{c<i} S[rho][c] S[i][c]   (rho = i: squared norm)
-    double a0 = 0.0, a1 = 0.0;
-    if (rho <= i) {
-      int cc = q;
-      for (; cc + Q < i; cc += 2 * Q) {
-        a0 = fma(S[rho + cc * lds], S[i + cc * lds], a0);
-        a1 = fma(S[rho + (cc + Q) * lds], S[i + (cc + Q) * lds], a1);
+  // ---- RQ (dgerq2): rows bottom to top; the reflector of row i acts on columns 0..i ----
+  // Warp 0 forms the reflectors: in round s it applies reflector s to row s-1 and forms reflector
+  // s-1 from it (the critical chain); warps 1.. apply reflector s to the rows below s-1 in the
+  // same round (FP64 throughput), so the two overlap.  They hand over through named barriers:
+  // ready[s&1] (reflector s published; warp 0 arrives, the others wait) and done[s&1] (rows below
+  // s-1 updated by reflector s; the others arrive, warp 0 waits before it touches row s-2).
+  // Same-parity generations never overlap: warp 0 publishes reflector r only after waiting for
+  // done(r+2), which the others signal after consuming ready(r+2); the others signal done(s) only
+  // after waiting for ready(s), which warp 0 publishes after consuming done(s+2).
+  {
+    const int nthr = blockDim.x, lane = t & 31;
+    double* pv = sc + 4;  // two published reflectors: v[0..L-1] (v_s = 1 implied), tau at [L]
+    auto bar_sync = [&](int id) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthr) : "memory"); };
+    auto bar_arrive = [&](int id) { asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(nthr) : "memory"); };
+    if (t < 32) {
+      // reflector of row r from its current values: scaled tail into S and the publish slot
+      auto form = [&](int r) {
+        double sg = 0.0;
+        for (int c = lane; c < r; c += 32) sg = fma(S[r + c * lds], S[r + c * lds], sg);
+        sg = warp_sum(sg);
+        const Reflector h = reflector_from_norm2(S[r + r * lds], sg);
+        double* v = pv + (r & 1) * (L + 1);
+        for (int c = lane; c < r; c += 32) {
+          const double x = S[r + c * lds] * h.scal;
+          S[r + c * lds] = x;
+          v[c] = x;
+        }
+        if (lane == 0) {
+          S[r + r * lds] = h.beta;
+          v[L] = h.tau;
+          tauR[r] = h.tau;
+        }
+      };
+      if (nb2 >= 1) form(nb2 - 1);
+      if (nb2 - 1 >= 1) {
+        __threadfence_block();
+        bar_arrive(1 + ((nb2 - 1) & 1));
       }
-      if (cc < i) a0 = fma(S[rho + cc * lds], S[i + cc * lds], a0);
-    }
-    const double d = group_sum<Q>(a0 + a1);
-    if (q == 0 && rho <= i) dvec[rho] = d;
-    if (rho == i && q == 0) {
-      const Reflector h = reflector_from_norm2(S[i + i * lds], d);
-      sc[0] = h.tau;
-      sc[1] = h.scal;
-      sc[2] = h.beta;
-    }
-    __syncthreads();
-    const double ti = sc[0], scal = sc[1], beta = sc[2];
-    if (rho < i && ti != 0.0) {
-      const double w = S[rho + i * lds] + scal * dvec[rho];
-      const double tw = ti * w, tws = tw * scal;
-      for (int cc = q; cc < i; cc += Q) S[rho + cc * lds] = fma(-tws, S[i + cc * lds], S[rho + cc * lds]);
-      if (q == 0) S[rho + i * lds] -= tw;
-    }
-    __syncthreads();
-    if (rho == i) {
-      for (int cc = q; cc < i; cc += Q) S[i + cc * lds] *= scal;
-      if (q == 0) {
-        S[i + i * lds] = beta;
-        tauR[i] = ti;
+      for (int sr = nb2 - 1; sr >= 1; --sr) {
+        if (sr <= nb2 - 2) bar_sync(3 + ((sr + 1) & 1));  // row sr-1 has reflector sr+1 applied
+        const double* v = pv + (sr & 1) * (L + 1);
+        const double tau = v[L];
+        const int r = sr - 1;
+        double d = 0.0;
+        for (int c = lane; c < sr; c += 32) d = fma(S[r + c * lds], v[c], d);
+        d = warp_sum(d);
+        if (tau != 0.0) {
+          const double tw = tau * (S[r + sr * lds] + d);
+          for (int c = lane; c < sr; c += 32) S[r + c * lds] = fma(-tw, v[c], S[r + c * lds]);
+          if (lane == 0) S[r + sr * lds] -= tw;
+        }
+        __syncwarp();
+        form(r);
+        if (r >= 1) {
+          __threadfence_block();
+          bar_arrive(1 + (r & 1));
+        }
+      }
+      if (nb2 - 1 >= 1) bar_sync(3 + (1 & 1));  // done(1)
+    } else {
+      const int u = t - 32, g = u / Q, qq = u % Q, G = (nthr - 32) / Q;
+      for (int sr = nb2 - 1; sr >= 1; --sr) {
+        bar_sync(1 + (sr & 1));
+        const double* v = pv + (sr & 1) * (L + 1);
+        const double tau = v[L];
+        for (int k0 = 0; k0 * G < sr - 1; ++k0) {  // uniform over the warps of this group
+          const int rr = g + G * k0;
+          double a0 = 0.0, a1 = 0.0;
+          if (rr < sr - 1) {
+            int cc = qq;
+            for (; cc + Q < sr; cc += 2 * Q) {
+              a0 = fma(S[rr + cc * lds], v[cc], a0);
+              a1 = fma(S[rr + (cc + Q) * lds], v[cc + Q], a1);
+            }
+            if (cc < sr) a0 = fma(S[rr + cc * lds], v[cc], a0);
+          }
+          const double dd = group_sum<Q>(a0 + a1);
+          if (rr < sr - 1 && tau != 0.0) {
+            const double tw = tau * (S[rr + sr * lds] + dd);
+            for (int cc = qq; cc < sr; cc += Q) S[rr + cc * lds] = fma(-tw, v[cc], S[rr + cc * lds]);
+            if (qq == 0) S[rr + sr * lds] -= tw;
+          }
+        }
+        __threadfence_block();
+        bar_arrive(3 + (sr & 1));
       }
     }
   }
@@ -364,10 +415,13 @@ size_t s1_lgen_smem(int L, int nb) {
 }
 static size_t s1_rgen_smem_vr(int L, int nb, bool vr) {
   const size_t p = (size_t)s1_rgen_pitch(L);
-  return sizeof(double) * (p * L + (size_t)nb * p + (vr ? (size_t)L * L : 0) + 2 * (size_t)L + nb + 2 * nb * nb + 4);
+  return sizeof(double) *
+         (p * L + (size_t)nb * p + (vr ? (size_t)L * L : 0) + 2 * (size_t)L + nb + 2 * nb * nb + 4 + 2 * ((size_t)L + 1));
 }
 size_t s1_rgen_smem(int L, int nb) { return s1_rgen_smem_vr(L, nb, false); }
-int s1_rgen_threads(int L) { return 4 * (((L + 7) / 8) * 8); }  // 4 lanes per row, multiple of 32
+// 4 lanes per row, a multiple of 32, and at least two warps (warp 0 forms the RQ reflectors, the
+// others update the remaining rows)
+int s1_rgen_threads(int L) { return max(64, 4 * (((L + 7) / 8) * 8)); }
 int s1_lgen_threads(int nb) { return ((8 * nb + 31) / 32) * 32; }  // 8 lanes per column
 
 void launch_s1_lgen(cudaStream_t s, double* A, int lda, const S1Panel& P, double* VL, double* TL) {

@@ -38,6 +38,7 @@ struct GeoS1Left {
   PHT_DEV int count() const { return P.nblocks; }
   PHT_DEV int slot_op(int s) const { return s; }
   PHT_DEV int op_slot(int o) const { return o; }
+  static constexpr int kSite = 0;  // stage-1 op list (kernel statistics)
   PHT_DEV bool masks_y() const { return false; }
   PHT_DEV void range(int, const WYOp& w, int, int& a, int& b) const {
     a = 0;
@@ -66,6 +67,7 @@ struct GeoS1Q {
   PHT_DEV int count() const { return P.nblocks; }
   PHT_DEV int slot_op(int s) const { return s; }
   PHT_DEV int op_slot(int o) const { return o; }
+  static constexpr int kSite = 0;  // stage-1 op list (kernel statistics)
   PHT_DEV bool masks_y() const { return false; }
   PHT_DEV void range(int, const WYOp& w, int, int& a, int& b) const {
     a = 0;
@@ -97,6 +99,7 @@ struct GeoS1Right {
   PHT_DEV int count() const { return bl_only >= 0 ? 1 : P.nblocks; }
   PHT_DEV int slot_op(int s) const { return s; }
   PHT_DEV int op_slot(int o) const { return o; }
+  static constexpr int kSite = 0;  // stage-1 op list (kernel statistics)
   PHT_DEV bool masks_y() const { return false; }
   PHT_DEV void range(int, const WYOp& w, int, int& a, int& b) const {
     a = 0;

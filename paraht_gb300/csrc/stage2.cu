@@ -48,6 +48,7 @@ struct GeoS2 {
   // Whether some row stops before the block's last reflector (the lookahead staircase): the
   // split kernel then forms Y = X T and masks it (wy_stream.cuh).
   PHT_DEV bool masks_y() const { return blk && kind == kLaRight; }
+  static constexpr int kSite = 1;  // stage-2 op list (kernel statistics)
   // Reflectors [a, b] (0-based) of op o applied to strip row `row` (0-based, lo <= row <= hi).
   PHT_DEV void range(int o, const WYOp& w, int row, int& a, int& b) const {
     a = 0;

@@ -16,7 +16,6 @@ namespace pht {
 constexpr int kApplyThreads = 256;
 constexpr int kLeftCS = 32;    // columns per CTA (left ops)
 constexpr int kLeftRCH = 128;  // row chunk staged in shared memory
-constexpr int kRightRS = 64;   // rows per CTA (right ops)
 constexpr int kRightCCH = 64;  // column chunk staged in shared memory
 constexpr int kMaxK = 64;      // max reflectors per op
 
@@ -104,8 +103,9 @@ __global__ void __launch_bounds__(kApplyThreads) k_apply_left(double* __restrict
   }
 }
 
-// X <- X H on rows [row0 + blockIdx.x*RS, ...] for every op (dlarfb 'R','N','F','C').
-template <class Geo>
+// X <- X H on rows [row0 + blockIdx.x*RS, ...] for every op (dlarfb 'R','N','F','C').  RS rows
+// per CTA: 64 for bulk lists; 8 for small critical-path updates, spreading them over more SMs.
+template <class Geo, int kRightRS = 64>
 __global__ void __launch_bounds__(kApplyThreads) k_apply_right(double* __restrict__ X, int ldx, int row0, int row1,
                                                                 Geo g) {
   extern __shared__ double smx[];
@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(kApplyThreads) k_apply_right(double* __restric
   if (rbeg > row1) return;
   const int rend = min(row1, rbeg + kRightRS - 1);
   const int nops = g.count();
-  constexpr int kGroups = kApplyThreads / kRightRS;  // 4
+  constexpr int kGroups = kApplyThreads / kRightRS;
   for (int o = 0; o < nops; ++o) {
     const WYOp op = g.op(o);
     const int ra = max(rbeg, op.lo), rb = min(rend, op.hi);
@@ -190,7 +190,8 @@ __global__ void __launch_bounds__(kApplyThreads) k_apply_right(double* __restric
 }
 
 constexpr size_t kLeftSmem = sizeof(double) * (size_t)(kLeftRCH + kMaxK) * (kLeftCS + 1);
-constexpr size_t kRightSmem = sizeof(double) * (size_t)(kRightCCH + kMaxK) * (kRightRS + 1);
+template <int RS>
+constexpr size_t right_smem() { return sizeof(double) * (size_t)(kRightCCH + kMaxK) * (RS + 1); }
 
 // Launch helpers: one CTA per strip; the dynamic shared-memory opt-in is set once per
 // instantiation.
@@ -206,17 +207,17 @@ inline void launch_apply_left(double* X, int ldx, int col0, int col1, const Geo&
   count_launch();
   k_apply_left<Geo><<<nblk, kApplyThreads, kLeftSmem, s>>>(X, ldx, col0, col1, g);
 }
-template <class Geo>
+template <class Geo, int RS = 64>
 inline void launch_apply_right(double* X, int ldx, int row0, int row1, const Geo& g, cudaStream_t s) {
   if (row1 < row0) return;
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_apply_right<Geo>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRightSmem);
+    cudaFuncSetAttribute(k_apply_right<Geo, RS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)right_smem<RS>());
     attr = true;
   }
-  const int nblk = (row1 - row0 + 1 + kRightRS - 1) / kRightRS;
+  const int nblk = (row1 - row0 + 1 + RS - 1) / RS;
   count_launch();
-  k_apply_right<Geo><<<nblk, kApplyThreads, kRightSmem, s>>>(X, ldx, row0, row1, g);
+  k_apply_right<Geo, RS><<<nblk, kApplyThreads, right_smem<RS>(), s>>>(X, ldx, row0, row1, g);
 }
 
 }  // namespace pht

@@ -38,6 +38,7 @@
 // Limits: k <= 16 reflectors, span len <= 64 per op.
 #pragma once
 #include <cuda_fp16.h>
+#include <stddef.h>
 #include <stdint.h>
 
 #include "launch_count.h"
@@ -55,12 +56,18 @@ constexpr int kWsThreads = 32 * kWsWarps;
 constexpr int kWsCW = 64;          // resident column slots per row (slot = column mod kWsCW)
 constexpr int kWsPL = kWsLen + 8;  // fp16 pitch of len-indexed digit rows (conflict-free)
 constexpr int kWsPK = kWsK + 8;    // fp16 pitch of k-indexed digit rows
+constexpr int kWsMM = 32;          // largest span with the one-product form C -= C M
+constexpr int kWsPM = kWsMM + 8;   // fp16 pitch of M's digit rows
 constexpr int kWsHead = 9;         // headroom bits of the row scale
 constexpr int kWsNoScale = -2000;  // row scale not set yet (no nonzero value loaded)
 
 // Operand digits of one op, prepared once per op (k_ws_prep) and copied to shared memory.  In the
-// two-product form vt/fvt hold W = T V^T by columns of W and td is unused.
+// two-product form vt/fvt hold W = T V^T by columns of W and td is unused; mt/fm (lists without
+// Y masks, len <= kWsMM) hold M = V W.
 struct WsOpDigits {
+  // C -= C M, M = V T V^T (len <= kWsMM): the whole op as one product (first: copied alone)
+  uint16_t mt[kWsD][kWsMM][kWsPM];   // M   [c_out][c_in]: B operand of C M
+  int fm[kWsMM];                     // scale of column c_out of M
   uint16_t vd[kWsD][kWsK][kWsPL];    // V   [m][c]: B operand of C V (FP16 bit patterns)
   uint16_t td[kWsD][kWsK][kWsPK];    // T   [m][l]: B operand of X T
   uint16_t vt[kWsD][kWsLen][kWsPK];  // V^T [c][m]: B operand of Y V^T
@@ -186,7 +193,9 @@ __global__ void __launch_bounds__(128) k_ws_prep(Geo g, WsOpDigits* out) {
   __shared__ double Vs[kWsLen][kWsK + 1];  // V[c][m]
   __shared__ double Tsh[kWsK][kWsK + 1];   // T[l][m]
   __shared__ double Wsh[kWsK][kWsLen + 1]; // W[m][c] (two-product form)
+  __shared__ double Msh[kWsMM][kWsMM + 1]; // M[c_in][c_out] = V W (one-product form)
   __shared__ int sc[kWsLen];
+  __shared__ int scv[kWsK];  // V's column scales (sc is reused for M's and W's columns)
   const int slot = blockIdx.x;
   const WYOp op = g.op(g.slot_op(slot));
   WsOpDigits* D = out + slot;
@@ -212,7 +221,7 @@ __global__ void __launch_bounds__(128) k_ws_prep(Geo g, WsOpDigits* out) {
     for (int o = 1; o < 8; o <<= 1) amax = max(amax, (uint64_t)__shfl_xor_sync(0xffffffffu, (long long)amax, o));
     if (part == 0) {
       D->fv[m] = ws_exp_bits(amax);
-      sc[m] = ws_exp_bits(amax);
+      scv[m] = ws_exp_bits(amax);
     }
   }
   // T's columns (three-product form); W = T V^T, eight independent sums per thread
@@ -235,10 +244,42 @@ __global__ void __launch_bounds__(128) k_ws_prep(Geo g, WsOpDigits* out) {
     for (int q = 0; q < 8; ++q) Wsh[m][c0 + 8 * q] = acc[q];
   }
   __syncthreads();
+  const bool one = two && len <= kWsMM;
+  if (one) {  // M = V W, eight independent sums per thread
+    const int ci = t & 31, co0 = t >> 5;  // columns co0, co0+4, ..., co0+28
+    double acc[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) acc[q] = 0.0;
+    for (int m = 0; m < kWsK; ++m) {
+      const double v = Vs[ci][m];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) acc[q] = fma(v, Wsh[m][co0 + 4 * q], acc[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) Msh[ci][co0 + 4 * q] = acc[q];
+    __syncthreads();
+    {  // scales of M's columns: 4 lanes per column
+      const int co = t >> 2, part = t & 3;
+      uint64_t amax = 0;
+      for (int c = part; c < kWsMM; c += 4) amax = max(amax, ws_abs_bits(Msh[c][co]));
+      amax = max(amax, (uint64_t)__shfl_xor_sync(0xffffffffu, (long long)amax, 1));
+      amax = max(amax, (uint64_t)__shfl_xor_sync(0xffffffffu, (long long)amax, 2));
+      if (part == 0) {
+        D->fm[co] = ws_exp_bits(amax);
+        sc[co] = ws_exp_bits(amax);
+      }
+    }
+    __syncthreads();
+    for (int e = t; e < kWsMM * kWsPM; e += 128) {
+      const int co = e / kWsPM, ci2 = e % kWsPM;
+      ws_put_digits(&D->mt[0][co][ci2], kWsMM * kWsPM, ci2 < kWsMM ? Msh[ci2][co] : 0.0, sc[co]);
+    }
+    __syncthreads();  // sc is reused below
+  }
   // V digits [m][c]
   for (int e = t; e < kWsK * kWsPL; e += 128) {
     const int m = e / kWsPL, c = e % kWsPL;
-    ws_put_digits(&D->vd[0][m][c], kWsK * kWsPL, c < kWsLen ? Vs[c][m] : 0.0, sc[m]);
+    ws_put_digits(&D->vd[0][m][c], kWsK * kWsPL, c < kWsLen ? Vs[c][m] : 0.0, scv[m]);
   }
   __syncthreads();  // sc is reused below
   // right factor of the last product by columns c: W (two-product form) or V^T
@@ -274,14 +315,16 @@ __global__ void __launch_bounds__(128) k_ws_prep(Geo g, WsOpDigits* out) {
 struct WsWarp {                                // per-warp bookkeeping (16 rows)
   int tag[kWsCW];                              // column held by each slot (-1: none)
   int newc[kWsLen];                            // op-relative columns loaded for the current op
+  int rmax[16];                                // largest exponent among a row's loaded values
 };
 struct WsSmem {
   WsOpDigits op;                               // the current op's operand digits
   long long win[kWsRows][kWsCW + 1];           // resident values (fixed point)
-  uint32_t dirty[kWsRows][(kWsCW + 31) / 32];  // modified since loaded
+  unsigned long long dirty[kWsRows];           // slots modified since loaded (one bit per slot)
   int escale[kWsRows];                         // row scales
   WsWarp w[kWsWarps];
 };
+static_assert(kWsCW == 64, "dirty masks hold one bit per slot");
 
 inline size_t ws_smem_bytes() { return sizeof(WsSmem); }
 
@@ -377,7 +420,8 @@ PHT_DEV void ws_to_afrag(__int128 (*xs)[2][2], const int (*xe)[2][2], int* emax,
 template <class Geo>
 __global__ void __launch_bounds__(kWsThreads, 2) k_ws_apply(double* __restrict__ C, long long rs, long long cs,
                                                             int row0, int row1, Geo g,
-                                                            const WsOpDigits* __restrict__ prep) {
+                                                            const WsOpDigits* __restrict__ prep,
+                                                            unsigned long long* __restrict__ flops) {
   extern __shared__ __align__(16) unsigned char ws_raw[];
   WsSmem& S = *reinterpret_cast<WsSmem*>(ws_raw);
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
@@ -392,7 +436,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_ws_apply(double* __restrict__
   for (int i = lane; i < kWsCW; i += 32) W.tag[i] = -1;
   if (lane < 16) {
     S.escale[wr0 + lane] = kWsNoScale;
-    for (int q = 0; q < (kWsCW + 31) / 32; ++q) S.dirty[wr0 + lane][q] = 0u;
+    S.dirty[wr0 + lane] = 0ull;
   }
   __syncwarp();
   const int nops = g.count();
@@ -403,106 +447,100 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_ws_apply(double* __restrict__
     const int ra = max(rbeg, op.lo), rb = min(rend, op.hi);
     if (ra > rb || op.k <= 0 || op.len <= 0) continue;  // CTA-uniform
     const int len = op.len, k = op.k;
-    __syncthreads();  // the previous op's digits are no longer read
-    {
-      const uint4* src = reinterpret_cast<const uint4*>(prep + g.op_slot(o));
-      uint4* dst = reinterpret_cast<uint4*>(&S.op);
-      for (int e = t; e < (int)(sizeof(WsOpDigits) / 16); e += kWsThreads) dst[e] = src[e];
-    }
-    __syncthreads();
-    // ---- reflector ranges of this lane's rows ----
+    // ---- reflector ranges of this lane's rows; which product form each warp takes ----
     int ra0 = 1, rb0 = 0, ra1 = 1, rb1 = 0;
     {
       const int r0 = grow0 + gq, r1 = grow0 + gq + 8;
       if (gq < nrows && r0 >= op.lo && r0 <= op.hi) g.range(o, op, r0, ra0, rb0);
       if (gq + 8 < nrows && r1 >= op.lo && r1 <= op.hi) g.range(o, op, r1, ra1, rb1);
     }
-    if (!__any_sync(0xffffffffu, ra0 <= rb0 || ra1 <= rb1)) continue;  // warp-uniform
-    // ---- make the op's columns resident (this warp's 16 rows) ----
-    int nn = 0;
-    for (int cc = 0; cc < len; ++cc) {
-      const int col = op.start + cc;
-      if (W.tag[col & (kWsCW - 1)] != col) {
-        if (lane == 0) W.newc[nn] = cc;
-        ++nn;
-      }
+    const bool on0 = ra0 <= rb0, on1 = ra1 <= rb1;
+    const bool wact = __any_sync(0xffffffffu, on0 || on1);
+    const bool full = (!on0 || (ra0 == 0 && rb0 == k - 1)) && (!on1 || (ra1 == 0 && rb1 == k - 1));
+    const bool wone = !ymask && len <= kWsMM && __all_sync(0xffffffffu, full);  // C -= C M
+    // the previous op's digits are no longer read; copy only the parts some warp needs
+    const int need_rest = __syncthreads_or(wact && !wone);
+    {
+      const size_t bytes = need_rest ? sizeof(WsOpDigits) : offsetof(WsOpDigits, vd);
+      const uint4* src = reinterpret_cast<const uint4*>(prep + g.op_slot(o));
+      uint4* dst = reinterpret_cast<uint4*>(&S.op);
+      for (int e = t; e < (int)(bytes / 16); e += kWsThreads) dst[e] = src[e];
     }
+    __syncthreads();
+    if (!wact) continue;  // warp-uniform
+    // ---- make the op's columns resident: new columns by ballot (two per lane) ----
+    int nn;
+    {
+      const int c0 = lane, c1 = lane + 32;
+      const bool n0 = c0 < len && W.tag[(op.start + c0) & (kWsCW - 1)] != op.start + c0;
+      const bool n1 = c1 < len && W.tag[(op.start + c1) & (kWsCW - 1)] != op.start + c1;
+      const uint32_t m0 = __ballot_sync(0xffffffffu, n0), m1 = __ballot_sync(0xffffffffu, n1);
+      const uint32_t below = (1u << lane) - 1u;
+      if (n0) W.newc[__popc(m0 & below)] = c0;
+      if (n1) W.newc[__popc(m0) + __popc(m1 & below)] = c1;
+      nn = __popc(m0) + __popc(m1);
+    }
+    if (lane < 16) W.rmax[lane] = kWsNoScale;
     __syncwarp();
-    for (int e = lane; e < nn * 16; e += 32) {  // evict dirty values of the slots' old columns
-      int i, rl;
-      if (cs == 1) {
-        i = e % nn;
-        rl = e / nn;
-      } else {
-        rl = e & 15;
-        i = e >> 4;
-      }
-      const int sl = (op.start + W.newc[i]) & (kWsCW - 1), rr = wr0 + rl;
+    // evict (write back the old column of the slot for dirty rows), load raw FP64 bits and note
+    // each row's largest exponent; lanes run along the contiguous direction of the matrix
+    for (int e = lane; e < nn * 16; e += 32) {
+      const int i = (cs == 1) ? e % nn : e >> 4, rl = (cs == 1) ? e / nn : e & 15;
+      const int col = op.start + W.newc[i], sl = col & (kWsCW - 1), rr = wr0 + rl;
       const int old = W.tag[sl];
-      const uint32_t bit = 1u << (sl & 31);
-      if (old >= 0 && rl < nrows && (S.dirty[rr][sl >> 5] & bit)) {
-        C[(long long)(grow0 + rl) * rs + (long long)old * cs] = ws_from_fixed(S.win[rr][sl], S.escale[rr]);
-        atomicAnd(&S.dirty[rr][sl >> 5], ~bit);
+      long long raw = 0;
+      if (rl < nrows) {
+        if (old >= 0 && ((S.dirty[rr] >> sl) & 1ull))
+          C[(long long)(grow0 + rl) * rs + (long long)old * cs] = ws_from_fixed(S.win[rr][sl], S.escale[rr]);
+        raw = __double_as_longlong(__ldcg(&C[(long long)(grow0 + rl) * rs + (long long)col * cs]));
+        const int ex = ws_exp_bits((uint64_t)raw & 0x7FFFFFFFFFFFFFFFull);
+        if (ex != kWsNoScale) atomicMax(&W.rmax[rl], ex);
       }
+      S.win[rr][sl] = raw;
     }
     __syncwarp();
-    for (int e0 = 0; e0 < nn * 16; e0 += 32 * 8) {  // load raw FP64 bits, eight loads in flight
-      long long raw[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int e = e0 + u * 32 + lane;
-        raw[u] = 0;
-        if (e < nn * 16) {
-          const int i = (cs == 1) ? e % nn : e >> 4, rl = (cs == 1) ? e / nn : e & 15;
-          if (rl < nrows)
-            raw[u] = __double_as_longlong(__ldcg(&C[(long long)(grow0 + rl) * rs + (long long)(op.start + W.newc[i]) * cs]));
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int e = e0 + u * 32 + lane;
-        if (e < nn * 16) {
-          const int i = (cs == 1) ? e % nn : e >> 4, rl = (cs == 1) ? e / nn : e & 15;
-          S.win[wr0 + rl][(op.start + W.newc[i]) & (kWsCW - 1)] = raw[u];
-        }
-      }
-    }
-    __syncwarp();
+    uint64_t newmask = 0;  // slots that now hold raw bits
+    for (int i = 0; i < nn; ++i) newmask |= 1ull << ((op.start + W.newc[i]) & (kWsCW - 1));
     for (int i = lane; i < nn; i += 32) W.tag[(op.start + W.newc[i]) & (kWsCW - 1)] = op.start + W.newc[i];
-    __syncwarp();
-    if (lane < nrows && nn > 0) {  // per row: raise the scale if needed, convert the loaded values
-      const int rr = wr0 + lane;
-      uint64_t amax = 0;
-      for (int i = 0; i < nn; ++i)
-        amax = max(amax, (uint64_t)(S.win[rr][(op.start + W.newc[i]) & (kWsCW - 1)] & 0x7FFFFFFFFFFFFFFFll));
-      const int ex = ws_exp_bits(amax);
-      int e = S.escale[rr];
+    if (lane < 16) S.dirty[wr0 + lane] &= ~newmask;  // freshly loaded entries are clean
+    if (lane < nrows) {  // raise a row's scale when a loaded value needs it (rare)
+      const int rr = wr0 + lane, ex = W.rmax[lane];
+      const int e = S.escale[rr];
       if (ex != kWsNoScale && (e == kWsNoScale || ex + kWsHead > e)) {
         const int enew = ex + kWsHead;
-        if (e != kWsNoScale) {  // shift the resident values that are not among the new ones
+        if (e != kWsNoScale) {
           const int sh = enew - e;
           for (int q = 0; q < kWsCW; ++q) {
-            const int col = W.tag[q];
-            if (col < 0) continue;
-            const int cc = col - op.start;
-            bool fresh = false;
-            if (cc >= 0 && cc < len)
-              for (int i = 0; i < nn; ++i) fresh = fresh || W.newc[i] == cc;
-            if (fresh) continue;
+            if (W.tag[q] < 0 || ((newmask >> q) & 1ull)) continue;
             const long long v = S.win[rr][q];
             const uint64_t s2 = ws_scale64((uint64_t)(v < 0 ? -v : v), -sh);
             S.win[rr][q] = v < 0 ? -(long long)s2 : (long long)s2;
           }
         }
-        e = enew;
-        S.escale[rr] = e;
-      }
-      for (int i = 0; i < nn; ++i) {
-        const int sl = (op.start + W.newc[i]) & (kWsCW - 1);
-        S.win[rr][sl] = ws_to_fixed(__longlong_as_double(S.win[rr][sl]), e);
+        S.escale[rr] = enew;
       }
     }
     __syncwarp();
+    for (int e = lane; e < nn * 16; e += 32) {  // convert the loaded values
+      const int i = (cs == 1) ? e % nn : e >> 4, rl = (cs == 1) ? e / nn : e & 15;
+      const int sl = (op.start + W.newc[i]) & (kWsCW - 1), rr = wr0 + rl;
+      if (rl < nrows) S.win[rr][sl] = ws_to_fixed(__longlong_as_double(S.win[rr][sl]), S.escale[rr]);
+    }
+    __syncwarp();
+    if (flops) {  // algorithmic work: 4 len k FP64-equivalent flops per active row
+      const int act = __popc(__ballot_sync(0xffffffffu, tq == 0 && on0)) + __popc(__ballot_sync(0xffffffffu, tq == 0 && on1));
+      if (lane == 0) atomicAdd(flops, (unsigned long long)act * 4ull * (unsigned long long)len * (unsigned long long)k);
+    }
+    // Only the entries an op modifies are written back: rows of a resident window that an op
+    // does not touch may be updated concurrently by other kernels on other streams (the next
+    // group's chase and lookahead), whose results a stale copy must not overwrite.
+    if (tq == 0) {  // the op's slots become dirty on the active rows
+      const unsigned long long span = len >= 64 ? ~0ull : ((1ull << len) - 1ull);
+      const int sh = op.start & (kWsCW - 1);
+      const unsigned long long opmask = sh ? ((span << sh) | (span >> (64 - sh))) : span;
+      if (on0) S.dirty[rA] |= opmask;
+      if (on1) S.dirty[rB] |= opmask;
+    }
     // ---- bit length of each row's largest value in the op's columns (4 lanes per row pair) ----
     const int lenp = (len + 15) & ~15;
     int blA, blB;
@@ -531,7 +569,65 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_ws_apply(double* __restrict__
     const int efix1 = gq + 8 < nrows ? S.escale[rB] : kWsNoScale;
     const int erow0 = (efix0 != kWsNoScale && blA > 0) ? efix0 - 62 + blA : kWsNoScale;
     const int erow1 = (efix1 != kWsNoScale && blB > 0) ? efix1 - 62 + blB : kWsNoScale;
-    // ---- X = C V (16 x k), exact levels per 32-column chunk; A fragments built in registers ----
+    // A fragments of C for one 16-column step at k0
+    auto cfrag = [&](int k0, uint32_t (*af)[4]) {
+      uint64_t F[8];
+      bool neg[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {  // fragment order: (A,k) (A,k+1) (B,k) (B,k+1) (A,k+8) ...
+        const int rowB = (i >> 1) & 1, cc = k0 + 2 * tq + (i & 1) + 8 * (i >> 2);
+        long long v = 0;
+        if (cc < len) v = S.win[rowB ? rB : rA][(op.start + cc) & (kWsCW - 1)];
+        neg[i] = v < 0;
+        F[i] = ws_scale64((uint64_t)(neg[i] ? -v : v), 56 - (rowB ? blB : blA));
+      }
+      ws_afrag(F, neg, af);
+    };
+    // C -= (correction levels in acc), columns c0 + nt*8 + 2tq + j; right-factor column scales fr,
+    // left digit scale zrow[hh]
+    auto correct = [&](const float (*acc)[2][4], int c0, const int* fr, const int* zrow, bool act0, bool act1) {
+#pragma unroll
+      for (int hh = 0; hh < 2; ++hh) {
+        if (!(hh ? act1 : act0)) continue;
+        const int rr = hh ? rB : rA;
+        const int er = hh ? efix1 : efix0, zr = zrow[hh];
+#pragma unroll
+        for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+          for (int j = 0; j < 2; ++j) {
+            const int cc = c0 + nt * 8 + 2 * tq + j;
+            if (cc >= len) continue;
+            const int fc = fr[cc];
+            if (fc == kWsNoScale) continue;
+            long long nh = 0, nl = 0;
+            ws_levels_of(acc, hh, nt, j, nh, nl);
+            if ((nh | nl) == 0) continue;
+            // correction in the row's fixed point: (nh 2^28 + nl) 2^sh, sh = zr + fc - 63 + 62 - er
+            const int sh = zr + fc - 1 - er;
+            const long long ah = nh < 0 ? -nh : nh, al = nl < 0 ? -nl : nl;
+            const long long dh = (long long)ws_scale64((uint64_t)ah, sh + 28);
+            const long long dl = (long long)ws_scale64((uint64_t)al, sh);
+            S.win[rr][(op.start + cc) & (kWsCW - 1)] -= (nh < 0 ? -dh : dh) + (nl < 0 ? -dl : dl);
+          }
+      }
+    };
+    if (wone) {
+      // ---- one product: C -= C M (len <= 32: two k-steps, two 16-column groups) ----
+      uint32_t af0[kWsD][4], af1[kWsD][4];
+      cfrag(0, af0);
+      if (lenp > 16) cfrag(16, af1);
+      const int zrow[2] = {erow0, erow1};
+      for (int c0 = 0; c0 < lenp; c0 += 16) {
+        float acc[kWsLv][2][4];
+        ws_zero_acc(acc);
+        ws_mma_step<kWsPM>(acc, af0, &S.op.mt[0][0][0], kWsMM * kWsPM, c0, 0, gq, tq);
+        if (lenp > 16) ws_mma_step<kWsPM>(acc, af1, &S.op.mt[0][0][0], kWsMM * kWsPM, c0, 16, gq, tq);
+        correct(acc, c0, S.op.fm, zrow, on0 && erow0 != kWsNoScale, on1 && erow1 != kWsNoScale);
+      }
+      __syncwarp();
+      continue;
+    }
+    // ---- X = C V (16 x k), exact levels per 32-column chunk ----
     long long xh[2][2][2], xl[2][2][2];  // [hh][nt][j]
 #pragma unroll
     for (int hh = 0; hh < 2; ++hh)
@@ -543,18 +639,8 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_ws_apply(double* __restrict__
       float acc[kWsLv][2][4];
       ws_zero_acc(acc);
       for (int k0 = kc; k0 < min(lenp, kc + 32); k0 += 16) {
-        uint64_t F[8];
-        bool neg[8];
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {  // fragment order: (A,k) (A,k+1) (B,k) (B,k+1) (A,k+8) ...
-          const int rowB = (i >> 1) & 1, cc = k0 + 2 * tq + (i & 1) + 8 * (i >> 2);
-          long long v = 0;
-          if (cc < len) v = S.win[rowB ? rB : rA][(op.start + cc) & (kWsCW - 1)];
-          neg[i] = v < 0;
-          F[i] = ws_scale64((uint64_t)(neg[i] ? -v : v), 56 - (rowB ? blB : blA));
-        }
         uint32_t af[kWsD][4];
-        ws_afrag(F, neg, af);
+        cfrag(k0, af);
         ws_mma_step<kWsPL>(acc, af, &S.op.vd[0][0][0], kWsK * kWsPL, 0, k0, gq, tq);
       }
 #pragma unroll
@@ -608,54 +694,21 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_ws_apply(double* __restrict__
       ws_to_afrag(xs, xe, zrow, zf);
     }
     // ---- C -= Z R (Z = X with R = W, or Z = Y with R = V^T), 16 columns at a time ----
-    const bool act0 = ra0 <= rb0 && zrow[0] != kWsNoScale, act1 = ra1 <= rb1 && zrow[1] != kWsNoScale;
+    const bool act0 = on0 && zrow[0] != kWsNoScale, act1 = on1 && zrow[1] != kWsNoScale;
     for (int c0 = 0; c0 < lenp; c0 += 16) {
       float acc[kWsLv][2][4];
       ws_zero_acc(acc);
       ws_mma_step<kWsPK>(acc, zf, &S.op.vt[0][0][0], kWsLen * kWsPK, c0, 0, gq, tq);
-#pragma unroll
-      for (int hh = 0; hh < 2; ++hh) {
-        if (!(hh ? act1 : act0)) continue;
-        const int rr = hh ? rB : rA;
-        const int er = hh ? efix1 : efix0, zr = zrow[hh];
-#pragma unroll
-        for (int nt = 0; nt < 2; ++nt)
-#pragma unroll
-          for (int j = 0; j < 2; ++j) {
-            const int cc = c0 + nt * 8 + 2 * tq + j;
-            if (cc >= len) continue;
-            const int fc = S.op.fvt[cc];
-            if (fc == kWsNoScale) continue;
-            long long nh = 0, nl = 0;
-            ws_levels_of(acc, hh, nt, j, nh, nl);
-            if ((nh | nl) == 0) continue;
-            // correction in the row's fixed point: (nh 2^28 + nl) 2^sh, sh = zr + fc - 63 + 62 - er
-            const int sh = zr + fc - 1 - er;
-            const long long ah = nh < 0 ? -nh : nh, al = nl < 0 ? -nl : nl;
-            const long long dh = (long long)ws_scale64((uint64_t)ah, sh + 28);
-            const long long dl = (long long)ws_scale64((uint64_t)al, sh);
-            const long long dv = (nh < 0 ? -dh : dh) + (nl < 0 ? -dl : dl);
-            const int sl = (op.start + cc) & (kWsCW - 1);
-            S.win[rr][sl] -= dv;
-            atomicOr(&S.dirty[rr][sl >> 5], 1u << (sl & 31));
-          }
-      }
+      correct(acc, c0, S.op.fvt, zrow, act0, act1);
     }
     __syncwarp();
   }
-  // ---- write back every dirty resident value ----
+  // ---- write back every modified resident value ----
   __syncwarp();
   for (int e = lane; e < kWsCW * 16; e += 32) {
-    int sl, rl;
-    if (cs == 1) {
-      sl = e % kWsCW;
-      rl = e / kWsCW;
-    } else {
-      rl = e & 15;
-      sl = e >> 4;
-    }
+    const int sl = (cs == 1) ? e % kWsCW : e >> 4, rl = (cs == 1) ? e / kWsCW : e & 15;
     const int col = W.tag[sl], rr = wr0 + rl;
-    if (col >= 0 && rl < nrows && (S.dirty[rr][sl >> 5] & (1u << (sl & 31))))
+    if (col >= 0 && rl < nrows && ((S.dirty[rr] >> sl) & 1ull))
       C[(long long)(grow0 + rl) * rs + (long long)col * cs] = ws_from_fixed(S.win[rr][sl], S.escale[rr]);
   }
 }
@@ -679,7 +732,13 @@ inline void launch_ws_apply(double* C, long long rs, long long cs, int row0, int
   }
   count_launch();
   const int nblk = (row1 - row0 + 1 + kWsRows - 1) / kWsRows;
-  k_ws_apply<Geo><<<nblk, kWsThreads, ws_smem_bytes(), s>>>(C, rs, cs, row0, row1, g, prep);
+  KernelClock* kc = tl_kclock;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  const bool timed = kc && kc->pair(Geo::kSite, &e0, &e1);
+  if (timed) cudaEventRecord(e0, s);
+  k_ws_apply<Geo><<<nblk, kWsThreads, ws_smem_bytes(), s>>>(C, rs, cs, row0, row1, g, prep,
+                                                              timed ? kc->dflops + Geo::kSite : nullptr);
+  if (timed) cudaEventRecord(e1, s);
 }
 
 }  // namespace pht

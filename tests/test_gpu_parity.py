@@ -185,3 +185,34 @@ def test_split_precision_reduce(oracle, ctx, n, r, p, nq, dist):
         assert abs_rel_max_diff(A, Ao) < 1e-8
         assert abs_rel_max_diff(B, Bo) < 1e-8
     assert ctx.launch_count() > 0
+
+
+def _dev_run(torch, fn, mats, *args):
+    n = mats[0].shape[0]
+    dev = [torch.from_numpy(np.ascontiguousarray(X.T)).cuda() for X in mats]
+    fn(n, dev[0].data_ptr(), n, dev[1].data_ptr(), n, dev[2].data_ptr(), n, dev[3].data_ptr(), n, *args)
+    torch.cuda.synchronize()
+    return [D.cpu().numpy().T for D in dev]
+
+
+@pytest.mark.parametrize("n,r,p,nq", [
+    (200, 8, 4, 8),    # stage 1 and 2 spans 32 / 16, k = 8: one-product form
+    (300, 16, 3, 8),   # stage-1 span 48 (two products), stage-2 span 24, k = 8
+    (300, 16, 4, 16),  # spans 64 / 32, k = 16
+    (257, 16, 2, 4),   # stage-1 span 32, stage-2 span 20, k = 4
+])
+def test_split_stages_match_fp64(ctx, n, r, p, nq):
+    """Each stage in split precision against the FP64 kernels on the same input: the split
+    kernels (one-, two- and three-product forms, staircase masks) perform the same transformations
+    to about FP64 accuracy."""
+    torch = pytest.importorskip("torch")
+    A0, B0 = make(n)
+    I = identity(n)
+    s1f = _dev_run(torch, ctx.ab2rht_d, [A0, B0, I, I], r, p, 0)
+    s1s = _dev_run(torch, ctx.ab2rht_d, [A0, B0, I, I], r, p, ph.PARAHT_FLAG_SPLIT)
+    for X, Y in zip(s1f, s1s):
+        assert rel_max_diff(Y, X) < 1e-10
+    s2f = _dev_run(torch, ctx.rht2ht_d, s1f, r, nq, 0)
+    s2s = _dev_run(torch, ctx.rht2ht_d, s1f, r, nq, ph.PARAHT_FLAG_SPLIT)
+    for X, Y in zip(s2f, s2s):
+        assert rel_max_diff(Y, X) < 1e-10
