@@ -45,6 +45,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("paraht", "reference"), default="paraht")
+    ap.add_argument("--workload", choices=("pencil", "batch4096"), default="pencil",
+                    help="pencil: one n x n pencil (the headline); batch4096: 4096 pencils, n ~ U{32..512}")
+    ap.add_argument("--loop-sample", type=int, default=256, help="pencils of the looped baseline (batch workload)")
     ap.add_argument("--n", type=int, default=16000)
     ap.add_argument("--r", type=int, default=16)
     ap.add_argument("--p", type=int, default=4)
@@ -104,6 +107,24 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
+def job_time(t_local: float, device) -> float:
+    """The job's step time: the maximum over ranks of each rank's own step time (replicas: every
+    rank reduces its own pencils, no data is exchanged; one all-reduce of a scalar)."""
+    import torch
+    import torch.distributed as td
+
+    if not (td.is_available() and td.is_initialized()) or td.get_world_size() == 1:
+        return t_local
+    tt = torch.tensor([t_local], dtype=torch.float64, device=device)
+    td.all_reduce(tt, op=td.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def replica_seed(base: int, rank: int) -> int:
+    """Seed of rank `rank`'s own input (replicas reduce different pencils of one distribution)."""
+    return base + rank
+
+
 def flops_nominal(n: int) -> float:
     # fixed nominal count used for "effective GFLOP/s" (stage 1 at p=8 plus stage 2): 18.67 n^3
     return 18.67 * float(n) ** 3
@@ -148,11 +169,192 @@ def run_reference(args, rank: int):
     return 0
 
 
+BATCH_METRIC = "batched HT reduction: pencils/s, 4096 pencils n~U{32..512}, FP64"
+
+
+def batch_params(n: int):
+    """(r, p, nq) of a batch pencil of size n (the persistent kernel takes p r <= 64)."""
+    return 16, 4, 16
+
+
+def run_batch(args, rank: int, world: int, local: int):
+    """--workload batch4096: 4096 FP64 pencils of uneven size (n ~ U{32..512}, seeded, Std) in one
+    paraht_reduce_batched_d call; the looped single-pencil path on a sample of the same pencils
+    and the CPU oracle on a smaller sample are timed beside it."""
+    from paraht_gb300.generate import batch_sizes, identity, pencil
+
+    count, lo, hi = 4096, 32, 512
+    sizes = batch_sizes(count, lo, hi, "uniform", seed=replica_seed(1302, rank))
+    params = [batch_params(n) for n in sizes]
+    flops = sum(18.67 * float(n) ** 3 for n in sizes)
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        from oracle import oracle as O
+
+        O.set_blas_threads(1)
+        sample = sizes[:16]
+        ts = []
+        for _ in range(max(1, args.steps)):
+            t0 = time.perf_counter()
+            for i, n in enumerate(sample):
+                A, B = pencil(n, "std", seed=7 + i)
+                r, p, nq = params[i]
+                O.reduce(A, B, identity(n), identity(n), min(r, n), p, min(nq, r))
+            ts.append(time.perf_counter() - t0)
+        v = len(sample) / statistics.mean(ts)
+        cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+        print(json.dumps({
+            "metric": BATCH_METRIC, "value": v, "unit": "pencils/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(ts) * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"batch of {count} pencils n~U{{{lo}..{hi}}} Std, r/p/nq=16/4/16"},
+            "cpu_baseline": {"value": v, "unit": "pencils/s", "cores": cores, "kind": "port",
+                             "sample": f"CPU oracle on the first {len(sample)} pencil sizes, one after the other"},
+            "e2e": {"value": v, "unit": "pencils/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}), flush=True)
+        return 0
+
+    import torch
+
+    import paraht_gb300 as ph
+
+    torch.cuda.set_device(local)
+    dist_on = world > 1
+    if dist_on:
+        import torch.distributed as td
+
+        td.init_process_group("nccl", device_id=torch.device("cuda", local))
+    host = [pencil(n, "std", seed=100000 * rank + i) for i, n in enumerate(sizes)]
+    pris = [[torch.from_numpy(np.ascontiguousarray(X.T)).cuda() for X in ab] for ab in host]
+    work = [[torch.empty_like(a), torch.empty_like(a), torch.empty_like(a), torch.empty_like(a)] for a, _ in pris]
+    eyes = {}
+    for n in set(sizes):
+        eyes[n] = torch.eye(n, dtype=torch.float64, device="cuda")
+    ctx = ph.Context(local)
+
+    def restore(idx):
+        for i in idx:
+            w, (a, b) = work[i], pris[i]
+            w[0].copy_(a)
+            w[1].copy_(b)
+            w[2].copy_(eyes[sizes[i]])
+            w[3].copy_(eyes[sizes[i]])
+        torch.cuda.synchronize()
+
+    def call(idx, flags):
+        ns = [sizes[i] for i in idx]
+        ptr = lambda j: [work[i][j].data_ptr() for i in idx]  # noqa: E731
+        ctx.reduce_batched_d(ns, ptr(0), ns, ptr(1), ns, ptr(2), ns, ptr(3), ns, [params[i][0] for i in idx],
+                             [params[i][1] for i in idx], [params[i][2] for i in idx], flags)
+
+    def barrier():
+        if dist_on:
+            import torch.distributed as td
+
+            td.barrier()
+
+    allidx = list(range(count))
+    for _ in range(args.warmup):
+        restore(allidx)
+        call(allidx, 0)
+    ts, launches = [], 0
+    sampler = ClockSampler(local)
+    with sampler:
+        for _ in range(args.steps):
+            restore(allidx)
+            barrier()
+            t0 = time.perf_counter()
+            call(allidx, 0)
+            ts.append(time.perf_counter() - t0)
+            launches += ctx.launch_count()
+            barrier()
+    t_step = statistics.mean(ts)
+    t_step = job_time(t_step, "cuda")
+    value = world * count / t_step
+    # looped baseline: the same call with PARAHT_FLAG_BATCH_LOOP on a sample of the batch
+    sample = allidx[: min(count, args.loop_sample)]
+    restore(sample)
+    t0 = time.perf_counter()
+    call(sample, ph.PARAHT_FLAG_BATCH_LOOP)
+    loop_v = len(sample) / (time.perf_counter() - t0)
+    # end to end: pinned host pencils -> device, batched call, results back (all four matrices)
+    hostp = [[torch.from_numpy(np.ascontiguousarray(X.T)).pin_memory() for X in ab] for ab in host]
+    outp = [[torch.empty(w[0].shape, dtype=torch.float64).pin_memory() for _ in range(4)] for w in work]
+    h2d = d2h = 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in allidx:
+        w = work[i]
+        w[0].copy_(hostp[i][0], non_blocking=True)
+        w[1].copy_(hostp[i][1], non_blocking=True)
+        w[2].copy_(eyes[sizes[i]])
+        w[3].copy_(eyes[sizes[i]])
+        h2d += 2 * w[0].numel() * 8
+    torch.cuda.synchronize()
+    call(allidx, 0)
+    for i in allidx:
+        for j in range(4):
+            outp[i][j].copy_(work[i][j], non_blocking=True)
+            d2h += work[i][j].numel() * 8
+    torch.cuda.synchronize()
+    e2e_v = world * count / (time.perf_counter() - t0)
+    # backward error spot check on a few pencils of the last call
+    errs = []
+    for i in allidx[:: max(1, count // 16)]:
+        A0, B0 = (torch.from_numpy(X) for X in host[i])
+        H, T, Q, Z = (torch.from_numpy(outp[i][j].numpy().T) for j in range(4))
+        errs.append(max(float(torch.linalg.norm(Q.T @ A0 @ Z - H) / torch.linalg.norm(A0)),
+                        float(torch.linalg.norm(Q.T @ B0 @ Z - T) / torch.linalg.norm(B0))))
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import oracle as O
+
+        O.set_blas_threads(1)
+        cs = sizes[:8]
+        t0 = time.perf_counter()
+        for i, n in enumerate(cs):
+            A, B = pencil(n, "std", seed=7 + i)
+            O.reduce(A, B, identity(n), identity(n), 16, 4, 16)
+        cpu = {"value": len(cs) / (time.perf_counter() - t0), "unit": "pencils/s",
+               "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)), "kind": "port",
+               "sample": f"CPU oracle on the first {len(cs)} pencil sizes of the batch, one after the other"}
+    if rank == 0:
+        achieved = flops / t_step / 1e12 * world
+        print(json.dumps({
+            "metric": BATCH_METRIC, "value": value, "unit": "pencils/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"batch of {count} pencils n~U{{{lo}..{hi}}} (seeded) Std, r/p/nq=16/4/16, FP64, "
+                                   f"one paraht_reduce_batched_d call",
+                       "pencils": count, "n_lo": lo, "n_hi": hi,
+                       "l2": "inputs ~12 GB >> L2; pristine inputs restored between steps outside the timed region"},
+            "e2e": {"value": e2e_v, "unit": "pencils/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "looped_baseline": {"value": loop_v, "unit": "pencils/s", "sample": len(sample),
+                                "speedup": value / world / loop_v},
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": 1.19, "unit": "TFLOP/s",
+                         "frac": achieved / 1.19, "traffic": None,
+                         "kernel": "k_batch_reduce (nominal 18.67 n^3 flops per pencil)",
+                         "peak_source": "FP64 FMA throughput measured on this pool's GB300 (fp64 probe)"},
+            "max_bwd_err_sampled": max(errs),
+            "cpu_baseline": cpu,
+            "clocks": sampler.summary(),
+        }), flush=True)
+    ctx.close()
+    if dist_on:
+        import torch.distributed as td
+
+        td.destroy_process_group()
+    return 0
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.workload != "pencil":
+        return run_batch(args, rank, world, local)
     if args.impl == "reference":
         return run_reference(args, rank)
 
@@ -178,7 +380,7 @@ def main():
 
     n, r, p, nq = args.n, args.r, args.p, args.nq
     flags = ph.PARAHT_FLAG_SPLIT if args.precision == "split" else 0
-    A0, B0 = pencil(n, args.dist, seed=1302 + rank)
+    A0, B0 = pencil(n, args.dist, seed=replica_seed(1302, rank))
     # pristine inputs on the device (column-major: a row-major tensor of the transpose)
     dev0 = [torch.from_numpy(np.ascontiguousarray(X.T)).cuda() for X in (A0, B0)]
     eye = torch.eye(n, dtype=torch.float64, device="cuda")
@@ -246,12 +448,7 @@ def main():
                     kst[k][f] += st[k][f]
             barrier()
     t_step = statistics.mean(ms) / 1e3
-    if dist_on:
-        import torch.distributed as td
-
-        tt = torch.tensor([t_step], device="cuda")
-        td.all_reduce(tt, op=td.ReduceOp.MAX)
-        t_step = float(tt.item())
+    t_step = job_time(t_step, "cuda")
     value = t_step / world
 
     # backward error of the last timed step (outside the timed region)
@@ -264,7 +461,7 @@ def main():
         check = {"bwd_err_A": ea, "bwd_err_B": eb, "bound_10n_eps": 10 * n * EPS}
 
     # end to end through the host entry point, copies inside the timed region
-    e2e_v = statistics.mean([host_step() for _ in range(max(1, args.e2e_steps))]) / world
+    e2e_v = statistics.mean([host_step() for _ in range(args.e2e_steps)]) / world if args.e2e_steps > 0 else None
 
     phases = None
     if args.phases:  # time_components serialises the streams: one extra, slower step
@@ -317,7 +514,8 @@ def main():
                        "n": n, "r": r, "p": p, "nq": nq, "precision": args.precision, "dist": args.dist,
                        "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs 8.2 GB >> L2; pristine input restored between steps outside the timed region"},
-            "e2e": {"value": e2e_v, "unit": "s", "h2d_bytes_per_step": 4 * n * n * 8, "d2h_bytes_per_step": 4 * n * n * 8},
+            "e2e": ({"value": e2e_v, "unit": "s", "h2d_bytes_per_step": 4 * n * n * 8, "d2h_bytes_per_step": 4 * n * n * 8}
+                    if e2e_v is not None else None),
             "gpu_launches": launches,
             "effective_gflops": flops_nominal(n) / t_step / 1e9,
             "roofline": roofline,

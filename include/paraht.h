@@ -124,7 +124,14 @@ int paraht_rht2ht_d_noalloc(paraht_ctx ctx, int n, double* A, int lda, double* B
 
 /* ---- batched: `count` independent pencils of possibly different sizes (device pointers).
  * Arrays of length count; r, p, nq per pencil.  No counterpart in the reference (it reduces one
- * pencil per run); the per-pencil arithmetic is that of paraht_reduce_d. ---- */
+ * pencil per run).  Pencils with p*r <= 64 and n <= PARAHT_BATCH_MAX_N are reduced by one
+ * persistent launch, one CTA per pencil at a time, largest first; their results are bitwise
+ * those of paraht_reduce_d in FP64 (also when PARAHT_FLAG_SPLIT is set).  The other pencils go
+ * through paraht_reduce_d one after the other, overlapping the persistent launch.
+ * PARAHT_FLAG_BATCH_LOOP sends every pencil through paraht_reduce_d (the looped baseline).
+ * Pointers of different pencils must not overlap. ---- */
+#define PARAHT_BATCH_MAX_N 1024
+#define PARAHT_FLAG_BATCH_LOOP 64
 int paraht_reduce_batched_d(paraht_ctx ctx, int count, const int* n, double* const* A, const int* lda,
                             double* const* B, const int* ldb, double* const* Q, const int* ldq, double* const* Z,
                             const int* ldz, const int* r, const int* p, const int* nq, int flags);

@@ -22,13 +22,14 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import (PARAHT_FLAG_CHECK_FINITE, PARAHT_FLAG_KERNEL_TIMES, PARAHT_FLAG_NO_ZERO_FILL,
-                   PARAHT_FLAG_SEQUENTIAL, PARAHT_FLAG_SPLIT, PARAHT_FLAG_TIME_COMPONENTS, ParahtError, check, lib)
+from ._lib import (PARAHT_BATCH_MAX_N, PARAHT_FLAG_BATCH_LOOP, PARAHT_FLAG_CHECK_FINITE, PARAHT_FLAG_KERNEL_TIMES,
+                   PARAHT_FLAG_NO_ZERO_FILL, PARAHT_FLAG_SEQUENTIAL, PARAHT_FLAG_SPLIT, PARAHT_FLAG_TIME_COMPONENTS,
+                   ParahtError, check, lib)
 
 __all__ = [
     "ab2rht_simple", "rht2ht_householder", "reduce", "Context", "ParahtError",
     "PARAHT_FLAG_TIME_COMPONENTS", "PARAHT_FLAG_CHECK_FINITE", "PARAHT_FLAG_SPLIT", "PARAHT_FLAG_NO_ZERO_FILL",
-    "PARAHT_FLAG_SEQUENTIAL", "PARAHT_FLAG_KERNEL_TIMES",
+    "PARAHT_FLAG_SEQUENTIAL", "PARAHT_FLAG_KERNEL_TIMES", "PARAHT_FLAG_BATCH_LOOP", "PARAHT_BATCH_MAX_N",
 ]
 
 PHASE_NAMES = ("s1_genleft", "s1_genright", "s1_mul", "s2_gen", "s2_lookahead", "s2_application", "copies", "total")

@@ -16,6 +16,8 @@ PARAHT_FLAG_SPLIT = 4
 PARAHT_FLAG_NO_ZERO_FILL = 8
 PARAHT_FLAG_SEQUENTIAL = 16
 PARAHT_FLAG_KERNEL_TIMES = 32
+PARAHT_FLAG_BATCH_LOOP = 64
+PARAHT_BATCH_MAX_N = 1024
 
 ERRORS = {
     -1001: "PARAHT_ERR_CUDA",

@@ -214,6 +214,11 @@ extern "C" int paraht_ctx_destroy(paraht_ctx c) {
     cudaStreamSynchronize(x.side2);
     cudaStreamDestroy(x.side2);
   }
+  if (x.bstream) {
+    cudaStreamSynchronize(x.bstream);
+    cudaStreamDestroy(x.bstream);
+  }
+  if (x.bws) cudaFree(x.bws);
   if (x.ev_a) cudaEventDestroy(x.ev_a);
   if (x.ev_b) cudaEventDestroy(x.ev_b);
   for (auto e : x.kc.ev) cudaEventDestroy(e);
@@ -587,12 +592,50 @@ extern "C" int paraht_reduce_batched_d(paraht_ctx c, int count, const int* n, do
     const int rc = check_args(3, 0, n[i], A[i], lda[i], B[i], ldb[i], Q[i], ldq[i], Z[i], ldz[i], r[i], p[i], nq[i]);
     if (rc) return -3;
   }
+  if (count == 0) return 0;
+  Ctx& x = c->c;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(x.device);
+  x.launches = 0;
+  const int single_flags = flags & ~(PARAHT_FLAG_TIME_COMPONENTS | PARAHT_FLAG_BATCH_LOOP | PARAHT_FLAG_KERNEL_TIMES);
+  std::vector<int> small, large;
   for (int i = 0; i < count; ++i) {
-    const int rc = paraht_reduce_d(c, n[i], A[i], lda[i], B[i], ldb[i], Q[i], ldq[i], Z[i], ldz[i], r[i], p[i], nq[i],
-                                   flags & ~PARAHT_FLAG_TIME_COMPONENTS);
-    if (rc) return rc;
+    if (n[i] == 0) continue;
+    const bool persistent = !(flags & PARAHT_FLAG_BATCH_LOOP) && n[i] <= PARAHT_BATCH_MAX_N &&
+                            pht::batch_eligible(n[i], r[i], p[i], nq[i]);
+    (persistent ? small : large).push_back(i);
   }
-  return 0;
+  int rc = 0;
+  long long launches = 0;
+  if (!small.empty()) {
+    if (!x.bstream && cudaStreamCreateWithFlags(&x.bstream, cudaStreamNonBlocking) != cudaSuccess) rc = PARAHT_ERR_CUDA;
+    if (!rc && (flags & PARAHT_FLAG_CHECK_FINITE))
+      for (int i : small) {
+        rc = pht::check_finite(x.stream, n[i], A[i], lda[i], B[i], ldb[i], x.dstatus);
+        if (rc) break;
+      }
+    if (!rc) {  // after everything queued on the context's stream
+      cudaEventRecord(x.ev_a, x.stream);
+      cudaStreamWaitEvent(x.bstream, x.ev_a, 0);
+      const long long l0 = pht::tl_launches;
+      rc = pht::batch_run(x, x.bstream, small, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, p, nq);
+      launches += pht::tl_launches - l0;
+    }
+  }
+  for (int i : large) {  // overlapping the persistent launch
+    if (rc) break;
+    rc = run_device(x, 3, n[i], A[i], lda[i], B[i], ldb[i], Q[i], ldq[i], Z[i], ldz[i], r[i], p[i], nq[i], single_flags);
+    launches += x.launches;
+  }
+  if (!small.empty() && x.bstream) {
+    const cudaError_t e = cudaStreamSynchronize(x.bstream);
+    if (!rc && e != cudaSuccess) rc = PARAHT_ERR_CUDA;
+  }
+  if (!rc) rc = finish(x);
+  x.launches = launches;
+  cudaSetDevice(prev);
+  return rc;
 }
 
 extern "C" const char* paraht_strerror(int s) {

@@ -85,6 +85,13 @@ struct Ctx {
     size_t used = 0;
   } kc;
   double kstats[6] = {0};
+  // persistent batched kernel (batched.cu): its device buffer (pencil table, queue counter,
+  // per-CTA workspace), the host image of the table, and the stream it runs on while the
+  // pencils it does not take go through the single-pencil path
+  void* bws = nullptr;
+  size_t bws_bytes = 0;
+  std::vector<char> bhost;
+  cudaStream_t bstream = nullptr;
 };
 
 size_t s1_workspace_bytes(int n, int nb, int p);
@@ -97,5 +104,11 @@ int s2_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
 // largest absolute value zeroed in dres[0] (A) and dres[1] (B).
 void zero_fill(cudaStream_t s, int n, double* A, int lda, int band, double* B, int ldb, double* dres);
 int check_finite(cudaStream_t s, int n, const double* A, int lda, const double* B, int ldb, int* dflag);
+// Batched reduction (batched.cu): which pencils the persistent kernel takes, and one launch
+// over the pencils idx[] of the batch on stream s.
+bool batch_eligible(int n, int r, int p, int nq);
+int batch_run(Ctx& x, cudaStream_t s, const std::vector<int>& idx, const int* n, double* const* A, const int* lda,
+              double* const* B, const int* ldb, double* const* Q, const int* ldq, double* const* Z, const int* ldz,
+              const int* r, const int* p, const int* nq);
 
 }  // namespace pht

@@ -17,7 +17,7 @@
 
 #include "paraht_internal.cuh"
 #include "paraht_impl.h"
-#include "stage1_geom.cuh"
+#include "stage1_gen.cuh"
 #include "split_apply.cuh"
 #include "wy_apply.cuh"
 
@@ -352,8 +352,6 @@ static size_t right_gen_small(int L, int nb) {
 }
 static size_t right_gen_big(int L, int nb) { return sizeof(double) * ((size_t)(L + 1) * L + (size_t)nb * (L + 1)); }
 
-size_t s1_lgen_smem(int L, int nb);
-size_t s1_rgen_smem(int L, int nb);
 void launch_s1_lgen(cudaStream_t s, double* A, int lda, const S1Panel& P, double* VL, double* TL);
 void launch_s1_rgen(cudaStream_t s, const double* B, int ldb, const S1Panel& P, int o, double* VRc, double* TR);
 
@@ -390,7 +388,7 @@ int s1_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
   // fast latency-oriented generation kernels (stage1_gen.cu) when the tiles fit; else the
   // general kernels above
   const bool fast_l = nb <= 64 && s1_lgen_smem(L, nb) <= (size_t)ctx.max_smem;
-  const bool fast_r = L <= 128 && s1_rgen_smem(L, nb) <= (size_t)ctx.max_smem;
+  const bool fast_r = L <= 128 && s1_rgen_smem_vr(L, nb, false) <= (size_t)ctx.max_smem;
   const size_t lsm = left_gen_smem(L, nb);
   const size_t rsm_small = right_gen_small(L, nb);
   const bool r_in_smem = rsm_small + right_gen_big(L, nb) <= (size_t)ctx.max_smem;

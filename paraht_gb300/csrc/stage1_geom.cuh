@@ -15,7 +15,7 @@ struct S1Panel {
   PHT_DEV __host__ int nb2(int o) const { return ib2(o) - ib(o) + 1; }
 };
 
-inline S1Panel make_panel(int n, int nb, int p, int jb0) {
+__host__ __device__ inline S1Panel make_panel(int n, int nb, int p, int jb0) {
   S1Panel g;
   g.n = n;
   g.nb = nb;

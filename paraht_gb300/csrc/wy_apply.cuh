@@ -19,17 +19,13 @@ constexpr int kLeftRCH = 128;  // row chunk staged in shared memory
 constexpr int kRightCCH = 64;  // column chunk staged in shared memory
 constexpr int kMaxK = 64;      // max reflectors per op
 
-// X <- H^T X on columns [col0 + blockIdx.x*CS, ...] for every op (dlarfb 'L','T','F','C').
+// X <- H^T X on the column strip [cbeg, cend] (at most kLeftCS columns) for every op
+// (dlarfb 'L','T','F','C'); kApplyThreads threads, shared memory kLeftSmem at smx.
 template <class Geo>
-__global__ void __launch_bounds__(kApplyThreads) k_apply_left(double* __restrict__ X, int ldx, int col0, int col1,
-                                                               Geo g) {
-  extern __shared__ double smx[];
+__device__ void apply_left_strip(double* __restrict__ X, int ldx, int cbeg, int cend, const Geo& g, double* smx) {
   double(*Xs)[kLeftCS + 1] = reinterpret_cast<double(*)[kLeftCS + 1]>(smx);
   double(*W)[kLeftCS + 1] = reinterpret_cast<double(*)[kLeftCS + 1]>(smx + kLeftRCH * (kLeftCS + 1));
   const int t = threadIdx.x;
-  const int cbeg = col0 + blockIdx.x * kLeftCS;
-  if (cbeg > col1) return;
-  const int cend = min(col1, cbeg + kLeftCS - 1);
   const int nops = g.count();
   for (int o = 0; o < nops; ++o) {
     const WYOp op = g.op(o);
@@ -103,18 +99,24 @@ __global__ void __launch_bounds__(kApplyThreads) k_apply_left(double* __restrict
   }
 }
 
-// X <- X H on rows [row0 + blockIdx.x*RS, ...] for every op (dlarfb 'R','N','F','C').  RS rows
-// per CTA: 64 for bulk lists; 8 for small critical-path updates, spreading them over more SMs.
-template <class Geo, int kRightRS = 64>
-__global__ void __launch_bounds__(kApplyThreads) k_apply_right(double* __restrict__ X, int ldx, int row0, int row1,
-                                                                Geo g) {
+template <class Geo>
+__global__ void __launch_bounds__(kApplyThreads) k_apply_left(double* __restrict__ X, int ldx, int col0, int col1,
+                                                               Geo g) {
   extern __shared__ double smx[];
+  const int cbeg = col0 + blockIdx.x * kLeftCS;
+  if (cbeg > col1) return;
+  apply_left_strip(X, ldx, cbeg, min(col1, cbeg + kLeftCS - 1), g, smx);
+}
+
+// X <- X H on the row strip [rbeg, rend] (at most kRightRS rows) for every op
+// (dlarfb 'R','N','F','C'); kApplyThreads threads, shared memory right_smem<kRightRS>() at smx.
+// Each row's arithmetic is the same for every strip height: RS = 64 for bulk lists, 8 for small
+// critical-path updates (spread over more SMs).
+template <class Geo, int kRightRS = 64>
+__device__ void apply_right_strip(double* __restrict__ X, int ldx, int rbeg, int rend, const Geo& g, double* smx) {
   double(*Xs)[kRightRS + 1] = reinterpret_cast<double(*)[kRightRS + 1]>(smx);
   double(*Y)[kRightRS + 1] = reinterpret_cast<double(*)[kRightRS + 1]>(smx + kRightCCH * (kRightRS + 1));
   const int t = threadIdx.x;
-  const int rbeg = row0 + blockIdx.x * kRightRS;
-  if (rbeg > row1) return;
-  const int rend = min(row1, rbeg + kRightRS - 1);
   const int nops = g.count();
   constexpr int kGroups = kApplyThreads / kRightRS;
   for (int o = 0; o < nops; ++o) {
@@ -187,6 +189,15 @@ __global__ void __launch_bounds__(kApplyThreads) k_apply_right(double* __restric
     }
     __syncthreads();
   }
+}
+
+template <class Geo, int kRightRS = 64>
+__global__ void __launch_bounds__(kApplyThreads) k_apply_right(double* __restrict__ X, int ldx, int row0, int row1,
+                                                                Geo g) {
+  extern __shared__ double smx[];
+  const int rbeg = row0 + blockIdx.x * kRightRS;
+  if (rbeg > row1) return;
+  apply_right_strip<Geo, kRightRS>(X, ldx, rbeg, min(row1, rbeg + kRightRS - 1), g, smx);
 }
 
 constexpr size_t kLeftSmem = sizeof(double) * (size_t)(kLeftRCH + kMaxK) * (kLeftCS + 1);

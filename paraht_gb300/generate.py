@@ -64,3 +64,14 @@ def pencil(n: int, dist: str = "std", seed: int = 1302):
 
 def identity(n: int):
     return np.asfortranarray(np.eye(n))
+
+
+def batch_sizes(count: int, lo: int, hi: int, law: str = "uniform", seed: int = 1302):
+    """Pencil sizes of a batch: n ~ U{lo..hi} (law "uniform") or n = floor(exp(U[ln lo, ln hi]))
+    (law "loguniform"), seeded."""
+    rng = np.random.default_rng(seed)
+    if law == "uniform":
+        return [int(v) for v in rng.integers(lo, hi + 1, size=count)]
+    if law == "loguniform":
+        return [int(np.floor(np.exp(v))) for v in rng.uniform(np.log(lo), np.log(hi), size=count)]
+    raise ValueError(f"unknown size law {law!r}")
