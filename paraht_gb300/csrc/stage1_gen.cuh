@@ -224,7 +224,7 @@ static __device__ void s1_rgen_body(const double* __restrict__ B, int ldb, const
       auto form = [&](int r) {
         double sg = 0.0;
         for (int c = lane; c < r; c += 32) sg = fma(S[r + c * lds], S[r + c * lds], sg);
-        sg = warp_sum(sg);
+        sg = warp_sum_fx(sg);
         const Reflector h = reflector_from_norm2(S[r + r * lds], sg);
         double* v = pv + (r & 1) * (L + 1);
         for (int c = lane; c < r; c += 32) {
@@ -250,7 +250,7 @@ static __device__ void s1_rgen_body(const double* __restrict__ B, int ldb, const
         const int r = sr - 1;
         double d = 0.0;
         for (int c = lane; c < sr; c += 32) d = fma(S[r + c * lds], v[c], d);
-        d = warp_sum(d);
+        d = warp_sum_fx(d);
         if (tau != 0.0) {
           const double tw = tau * (S[r + sr * lds] + d);
           for (int c = lane; c < sr; c += 32) S[r + c * lds] = fma(-tw, v[c], S[r + c * lds]);
@@ -299,9 +299,11 @@ static __device__ void s1_rgen_body(const double* __restrict__ B, int ldb, const
   if (nb2 > nb) {
     // ---- M = [I 0] H(1) H(2) ... H(nb2): first nb rows of the RQ orthogonal factor (dorgrq) ----
     // thread (row r = t / QM, part = t % QM) with QM lanes per row: the largest power of two
-    // <= min(32, qm_threads / nb) (qm_threads <= blockDim.x; it fixes the summation order)
+    // <= min(32, min(qm_threads, 128) / nb) (qm_threads <= blockDim.x; it fixes the summation
+    // order).  At most four warps, one per scheduler: each SM sub-partition issues one FP64
+    // instruction per ~64 cycles, so more warps with partly masked lanes only queue behind it.
     int QM = 1;
-    while (2 * QM <= 32 && 2 * QM * nb <= qm_threads) QM *= 2;
+    while (2 * QM <= 32 && 2 * QM * nb <= min(qm_threads, 128)) QM *= 2;
     const int r = t / QM, part = t % QM;
     for (int e = t; e < nb * nb2; e += blockDim.x) M[(e / nb2) * ldm + e % nb2] = ((e / nb2) == (e % nb2)) ? 1.0 : 0.0;
     if (use_vr)  // reflector of row i: S[i][0..i-1], implicit 1 at column i
