@@ -31,53 +31,6 @@ PHT_DEV double warp_sum(double v) {
   return v;
 }
 
-// Warp-wide sum through 64-bit fixed point: every lane's value is converted to an integer at the
-// scale of the warp's largest exponent (|v| < 2^57, so 32 of them cannot overflow), the integers
-// are summed exactly with shuffles and 64-bit integer adds, and the total is rounded to FP64 once.
-// On GB300 each dependent FP64 add costs about 64 cycles, so this replaces five of them on the
-// latency-critical reductions of the serial factorisations.  The only roundings are those of
-// the terms' bits below 2^-57 of the largest term (at most 32 half-units, 2^-53 of it in total)
-// and the final rounding of the exact total, so the result is at least as accurate as the FP64
-// butterfly's.  Non-finite inputs take the FP64 butterfly (NaN/Inf propagate).
-PHT_DEV double warp_sum_fx(double v) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-  const unsigned ex = (unsigned)(b >> 52) & 0x7FFu;
-  const unsigned emax = __reduce_max_sync(0xffffffffu, ex);
-  if (emax == 0x7FFu || emax == 0u) return warp_sum(v);  // non-finite, or only zeros/subnormals
-  // v = m 2^(e - 1075) with e = max(ex, 1);  fixed point f = v 2^(1079 - emax) = m 2^(e - emax + 4)
-  const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (ex ? (1ull << 52) : 0ull);
-  const int s = (int)(ex ? ex : 1u) - (int)emax + 4;  // <= 4
-  unsigned long long a;
-  if (s >= 0)
-    a = m << s;
-  else if (s > -64)
-    a = (m + (1ull << (-s - 1))) >> (-s);
-  else
-    a = 0;
-  long long f = (b >> 63) ? -(long long)a : (long long)a;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) f += __shfl_xor_sync(0xffffffffu, f, o);
-  if (f == 0) return 0.0;
-  // |f| < 2^62: round to 53 bits and assemble f 2^(emax - 1079)
-  const unsigned long long sign = (unsigned long long)f & 0x8000000000000000ull;
-  unsigned long long u = (unsigned long long)(f < 0 ? -f : f);
-  int msb = 63 - __clzll((long long)u);
-  unsigned long long mant;
-  if (msb > 52) {
-    const int sh = msb - 52;
-    mant = (u + (1ull << (sh - 1))) >> sh;
-    if (mant >> 53) {
-      mant >>= 1;
-      ++msb;
-    }
-  } else {
-    mant = u << (52 - msb);
-  }
-  const int e = msb + (int)emax - 1079;  // unbiased exponent of the result
-  if (e < -1022) return warp_sum(v);     // subnormal result: rare, take the FP64 path
-  return __longlong_as_double((long long)(sign | ((unsigned long long)(e + 1023) << 52) | (mant & 0xFFFFFFFFFFFFFull)));
-}
-
 PHT_DEV double block_sum(double v, double* red) {
   v = warp_sum(v);
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;

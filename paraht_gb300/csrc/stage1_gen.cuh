@@ -175,6 +175,55 @@ static __device__ void s1_lgen_body(double* __restrict__ A, int lda, const S1Pan
   }
 }
 
+// M <- M H(0) H(1) ... H(nb2-1) for the nb rows of M (dorgrq), QM lanes per row, the row held in
+// registers (column part + QM k in element k; nb2 <= 64).  Reflector i: V[i][c] at
+// Vs[i * vsi + c * vsc] for c < i, 1 at c = i, tau tauR[i].  Only the warps that own rows run.
+template <int QM>
+static __device__ void dorgrq_rows(double* M, int ldm, const double* Vs, int vsi, int vsc, const double* tauR, int nb,
+                                   int nb2) {
+  constexpr int EL = 64 / QM;
+  const int t = threadIdx.x, r = t / QM, part = t % QM;
+  if ((t & ~31) >= nb * QM) return;  // warp-uniform: no row of this warp exists
+  const bool live = r < nb;
+  double m[EL];
+#pragma unroll
+  for (int k = 0; k < EL; ++k) {
+    const int col = part + QM * k;
+    m[k] = (live && col < nb2) ? M[r * ldm + col] : 0.0;
+  }
+  for (int i = 0; i < nb2; ++i) {
+    const double ti = tauR[i];
+    if (ti == 0.0) continue;
+    double vv[EL];
+    double s0 = 0.0, s1 = 0.0;
+#pragma unroll
+    for (int k = 0; k < EL; ++k) {
+      vv[k] = 0.0;
+      if (QM * k <= i) {  // warp-uniform: some lane of this chunk lies at or before column i
+        const int col = part + QM * k;
+        vv[k] = col < i ? Vs[i * vsi + col * vsc] : (col == i ? 1.0 : 0.0);
+        if (k & 1)
+          s1 = fma(m[k], vv[k], s1);
+        else
+          s0 = fma(m[k], vv[k], s0);
+      }
+    }
+    double s = s0 + s1;
+#pragma unroll
+    for (int off = 1; off < QM; off <<= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    const double tw = ti * s;
+#pragma unroll
+    for (int k = 0; k < EL; ++k)
+      if (QM * k <= i) m[k] = fma(-tw, vv[k], m[k]);
+  }
+  if (live)
+#pragma unroll
+    for (int k = 0; k < EL; ++k) {
+      const int col = part + QM * k;
+      if (col < nb2) M[r * ldm + col] = m[k];
+    }
+}
+
 // ------------------------------------------------------------------------------------------
 // Right generation for block o.  blockDim.x == 4 * Lp (Lp = L rounded up to a multiple of 8);
 // thread (row rho = t/4, quarter q = t%4) owns columns c = q, q+4, q+8, ... of row rho.
@@ -224,7 +273,7 @@ static __device__ void s1_rgen_body(const double* __restrict__ B, int ldb, const
       auto form = [&](int r) {
         double sg = 0.0;
         for (int c = lane; c < r; c += 32) sg = fma(S[r + c * lds], S[r + c * lds], sg);
-        sg = warp_sum_fx(sg);
+        sg = warp_sum(sg);
         const Reflector h = reflector_from_norm2(S[r + r * lds], sg);
         double* v = pv + (r & 1) * (L + 1);
         for (int c = lane; c < r; c += 32) {
@@ -244,13 +293,13 @@ static __device__ void s1_rgen_body(const double* __restrict__ B, int ldb, const
         bar_arrive(1 + ((nb2 - 1) & 1));
       }
       for (int sr = nb2 - 1; sr >= 1; --sr) {
-        if (sr <= nb2 - 2) bar_sync(3 + ((sr + 1) & 1));  // row sr-1 has reflector sr+1 applied
+        if (sr <= nb2 - 2) bar_sync(3 + ((sr + 1) & 1));
         const double* v = pv + (sr & 1) * (L + 1);
         const double tau = v[L];
         const int r = sr - 1;
         double d = 0.0;
         for (int c = lane; c < sr; c += 32) d = fma(S[r + c * lds], v[c], d);
-        d = warp_sum_fx(d);
+        d = warp_sum(d);
         if (tau != 0.0) {
           const double tw = tau * (S[r + sr * lds] + d);
           for (int c = lane; c < sr; c += 32) S[r + c * lds] = fma(-tw, v[c], S[r + c * lds]);
@@ -312,26 +361,45 @@ static __device__ void s1_rgen_body(const double* __restrict__ B, int ldb, const
         Vr[i * L + cc] = cc < i ? S[i + cc * lds] : 0.0;
       }
     __syncthreads();
-    // rows of M are independent: each lane group runs through all reflectors without barriers
-    for (int i = 0; i < nb2; ++i) {
+    // rows of M are independent: each lane group runs through all reflectors without barriers,
+    // its row in registers when it fits (nb2 <= 64)
+    const int vsi = use_vr ? L : 1, vsc = use_vr ? 1 : lds;
+    const double* Vsrc = use_vr ? Vr : S;
+    bool done = false;
+    if (nb2 <= 64) {
+      switch (QM) {
+        case 4:
+          dorgrq_rows<4>(M, ldm, Vsrc, vsi, vsc, tauR, nb, nb2);
+          done = true;
+          break;
+        case 8:
+          dorgrq_rows<8>(M, ldm, Vsrc, vsi, vsc, tauR, nb, nb2);
+          done = true;
+          break;
+        case 16:
+          dorgrq_rows<16>(M, ldm, Vsrc, vsi, vsc, tauR, nb, nb2);
+          done = true;
+          break;
+        case 32:
+          dorgrq_rows<32>(M, ldm, Vsrc, vsi, vsc, tauR, nb, nb2);
+          done = true;
+          break;
+        default: break;
+      }
+    }
+    for (int i = 0; i < nb2 && !done; ++i) {
       const double ti = tauR[i];
       if (ti == 0.0) continue;
       double s = 0.0;
       if (r < nb) {
-        if (use_vr)
-          for (int cc = part; cc < i; cc += QM) s = fma(M[r * ldm + cc], Vr[i * L + cc], s);
-        else
-          for (int cc = part; cc < i; cc += QM) s = fma(M[r * ldm + cc], S[i + cc * lds], s);
+        for (int cc = part; cc < i; cc += QM) s = fma(M[r * ldm + cc], Vsrc[i * vsi + cc * vsc], s);
         if (part == 0) s += M[r * ldm + i];
       }
       // reduce over the QM lanes of this row (QM divides 32)
       for (int off = 1; off < QM; off <<= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
       if (r < nb) {
         const double tw = ti * s;
-        if (use_vr)
-          for (int cc = part; cc < i; cc += QM) M[r * ldm + cc] = fma(-tw, Vr[i * L + cc], M[r * ldm + cc]);
-        else
-          for (int cc = part; cc < i; cc += QM) M[r * ldm + cc] = fma(-tw, S[i + cc * lds], M[r * ldm + cc]);
+        for (int cc = part; cc < i; cc += QM) M[r * ldm + cc] = fma(-tw, Vsrc[i * vsi + cc * vsc], M[r * ldm + cc]);
         if (part == 0) M[r * ldm + i] -= tw;
       }
     }

@@ -40,6 +40,8 @@ struct GeoS1Left {
   PHT_DEV int op_slot(int o) const { return o; }
   static constexpr int kSite = 0;  // stage-1 op list (kernel statistics)
   PHT_DEV bool masks_y() const { return false; }
+  // every op applies all its reflectors to every row; one product C -= C M when spans are <= 32
+  __host__ __device__ bool one_product_only() const { return P.L <= 32; }
   PHT_DEV void range(int, const WYOp& w, int, int& a, int& b) const {
     a = 0;
     b = w.k - 1;
@@ -69,6 +71,8 @@ struct GeoS1Q {
   PHT_DEV int op_slot(int o) const { return o; }
   static constexpr int kSite = 0;  // stage-1 op list (kernel statistics)
   PHT_DEV bool masks_y() const { return false; }
+  // every op applies all its reflectors to every row; one product C -= C M when spans are <= 32
+  __host__ __device__ bool one_product_only() const { return P.L <= 32; }
   PHT_DEV void range(int, const WYOp& w, int, int& a, int& b) const {
     a = 0;
     b = w.k - 1;
@@ -101,6 +105,8 @@ struct GeoS1Right {
   PHT_DEV int op_slot(int o) const { return o; }
   static constexpr int kSite = 0;  // stage-1 op list (kernel statistics)
   PHT_DEV bool masks_y() const { return false; }
+  // every op applies all its reflectors to every row; one product C -= C M when spans are <= 32
+  __host__ __device__ bool one_product_only() const { return P.L <= 32; }
   PHT_DEV void range(int, const WYOp& w, int, int& a, int& b) const {
     a = 0;
     b = w.k - 1;

@@ -305,7 +305,7 @@ static __device__ double opposite_reflector(int nb, int ldb, Sm& s) {
       // v_i = [Bc(i, 0:i-1), 1, 0...]
       const double v0 = (t < i) ? Bc[i + t * ldb] : (t == i ? 1.0 : 0.0);
       const double v1 = (t + 32 < i) ? Bc[i + (t + 32) * ldb] : (t + 32 == i ? 1.0 : 0.0);
-      const double w = warp_sum_fx(fma(q0, v0, q1 * v1));
+      const double w = gsum<32>(fma(q0, v0, q1 * v1));
       const double tw = ti * w;
       q0 = fma(-tw, v0, q0);
       q1 = fma(-tw, v1, q1);

@@ -32,6 +32,12 @@ struct GeoS2 {
   // Whether some row stops before the block's last reflector (the lookahead staircase): the
   // split kernel then forms Y = X T and masks it (wy_stream.cuh).
   PHT_DEV bool masks_y() const { return blk && kind == kLaRight; }
+  // Whether every op of the list applies all its reflectors to every row over a span of at most
+  // 32 columns (the split kernel's one-product form C -= C M): the left lists and Q, Z.
+  __host__ __device__ bool one_product_only() const {
+    const bool full = kind == kUpQ || kind == kUpZ || kind == kUpLeft || kind == kLaLeftA || kind == kLaLeftB;
+    return full && r + nq <= 32;
+  }
   static constexpr int kSite = 1;  // stage-2 op list (kernel statistics)
   // Reflectors [a, b] (0-based) of op o applied to strip row `row` (0-based, lo <= row <= hi).
   PHT_DEV void range(int o, const WYOp& w, int row, int& a, int& b) const {

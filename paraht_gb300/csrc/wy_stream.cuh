@@ -41,6 +41,8 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "launch_count.h"
 #include "paraht_internal.cuh"
 
@@ -317,8 +319,17 @@ struct WsWarp {                                // per-warp bookkeeping (16 rows)
   int newc[kWsLen];                            // op-relative columns loaded for the current op
   int rmax[16];                                // largest exponent among a row's loaded values
 };
-struct WsSmem {
-  WsOpDigits op;                               // the current op's operand digits
+// The one-product operands alone (the leading members of WsOpDigits).
+struct WsOpM {
+  uint16_t mt[kWsD][kWsMM][kWsPM];
+  int fm[kWsMM];
+};
+static_assert(sizeof(WsOpM) == offsetof(WsOpDigits, vd), "WsOpM is the prefix of WsOpDigits");
+// kOne: every op of the list takes the one-product form (full reflector ranges, len <= kWsMM),
+// so only M's digits are staged: 57 KB instead of 104 KB, three CTAs per SM.
+template <bool kOne>
+struct WsSmemT {
+  typename std::conditional<kOne, WsOpM, WsOpDigits>::type op;  // the current op's operand digits
   long long win[kWsRows][kWsCW + 1];           // resident values (fixed point)
   unsigned long long dirty[kWsRows];           // slots modified since loaded (one bit per slot)
   int escale[kWsRows];                         // row scales
@@ -326,7 +337,8 @@ struct WsSmem {
 };
 static_assert(kWsCW == 64, "dirty masks hold one bit per slot");
 
-inline size_t ws_smem_bytes() { return sizeof(WsSmem); }
+template <bool kOne>
+inline size_t ws_smem_bytes() { return sizeof(WsSmemT<kOne>); }
 
 // round(a 2^s), a < 2^62, 64-bit only
 PHT_DEV uint64_t ws_scale64(uint64_t a, int s) {
@@ -417,13 +429,12 @@ PHT_DEV void ws_to_afrag(__int128 (*xs)[2][2], const int (*xe)[2][2], int* emax,
   ws_afrag(F, neg, af);
 }
 
-template <class Geo>
-__global__ void __launch_bounds__(kWsThreads, 2) k_ws_apply(double* __restrict__ C, long long rs, long long cs,
-                                                            int row0, int row1, Geo g,
-                                                            const WsOpDigits* __restrict__ prep,
-                                                            unsigned long long* __restrict__ flops) {
+template <class Geo, bool kOne>
+__global__ void __launch_bounds__(kWsThreads, kOne ? 3 : 2)
+    k_ws_apply(double* __restrict__ C, long long rs, long long cs, int row0, int row1, Geo g,
+               const WsOpDigits* __restrict__ prep, unsigned long long* __restrict__ flops) {
   extern __shared__ __align__(16) unsigned char ws_raw[];
-  WsSmem& S = *reinterpret_cast<WsSmem*>(ws_raw);
+  WsSmemT<kOne>& S = *reinterpret_cast<WsSmemT<kOne>*>(ws_raw);
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const int gq = lane >> 2, tq = lane & 3;
   const int rbeg = row0 + blockIdx.x * kWsRows;
@@ -457,9 +468,11 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_ws_apply(double* __restrict__
     const bool on0 = ra0 <= rb0, on1 = ra1 <= rb1;
     const bool wact = __any_sync(0xffffffffu, on0 || on1);
     const bool full = (!on0 || (ra0 == 0 && rb0 == k - 1)) && (!on1 || (ra1 == 0 && rb1 == k - 1));
-    const bool wone = !ymask && len <= kWsMM && __all_sync(0xffffffffu, full);  // C -= C M
+    // C -= C M; a kOne list guarantees it (checked on the host)
+    const bool wone = kOne || (!ymask && len <= kWsMM && __all_sync(0xffffffffu, full));
     // the previous op's digits are no longer read; copy only the parts some warp needs
-    const int need_rest = __syncthreads_or(wact && !wone);
+    const int need_rest = kOne ? 0 : __syncthreads_or(wact && !wone);
+    if (kOne) __syncthreads();
     {
       const size_t bytes = need_rest ? sizeof(WsOpDigits) : offsetof(WsOpDigits, vd);
       const uint4* src = reinterpret_cast<const uint4*>(prep + g.op_slot(o));
@@ -627,6 +640,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_ws_apply(double* __restrict__
       __syncwarp();
       continue;
     }
+    if constexpr (!kOne) {
     // ---- X = C V (16 x k), exact levels per 32-column chunk ----
     long long xh[2][2][2], xl[2][2][2];  // [hh][nt][j]
 #pragma unroll
@@ -702,6 +716,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_ws_apply(double* __restrict__
       correct(acc, c0, S.op.fvt, zrow, act0, act1);
     }
     __syncwarp();
+    }  // !kOne
   }
   // ---- write back every modified resident value ----
   __syncwarp();
@@ -717,15 +732,24 @@ inline bool ws_fits(int k_max, int len_max) { return k_max <= kWsK && len_max <=
 
 // Prepares the op list (nslots prep slots, Geo::slot_op; skipped when prepare is false) and
 // applies it to strip rows [row0, row1] of C viewed with strides (rs, cs).
+template <class Geo, bool kOne>
+inline void ws_set_smem_attr() {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_ws_apply<Geo, kOne>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ws_smem_bytes<kOne>());
+    attr = true;
+  }
+}
+
 template <class Geo>
 inline void launch_ws_apply(double* C, long long rs, long long cs, int row0, int row1, const Geo& g, int nslots,
                             WsOpDigits* prep, cudaStream_t s, bool prepare = true) {
   if (row1 < row0 || nslots <= 0) return;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_ws_apply<Geo>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ws_smem_bytes());
-    attr = true;
-  }
+  const bool one = g.one_product_only();
+  if (one)
+    ws_set_smem_attr<Geo, true>();
+  else
+    ws_set_smem_attr<Geo, false>();
   if (prepare) {
     count_launch();
     k_ws_prep<Geo><<<nslots, 128, 0, s>>>(g, prep);
@@ -736,8 +760,11 @@ inline void launch_ws_apply(double* C, long long rs, long long cs, int row0, int
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   const bool timed = kc && kc->pair(Geo::kSite, &e0, &e1);
   if (timed) cudaEventRecord(e0, s);
-  k_ws_apply<Geo><<<nblk, kWsThreads, ws_smem_bytes(), s>>>(C, rs, cs, row0, row1, g, prep,
-                                                              timed ? kc->dflops + Geo::kSite : nullptr);
+  unsigned long long* fl = timed ? kc->dflops + Geo::kSite : nullptr;
+  if (one)
+    k_ws_apply<Geo, true><<<nblk, kWsThreads, ws_smem_bytes<true>(), s>>>(C, rs, cs, row0, row1, g, prep, fl);
+  else
+    k_ws_apply<Geo, false><<<nblk, kWsThreads, ws_smem_bytes<false>(), s>>>(C, rs, cs, row0, row1, g, prep, fl);
   if (timed) cudaEventRecord(e1, s);
 }
 
