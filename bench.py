@@ -45,9 +45,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("paraht", "reference"), default="paraht")
-    ap.add_argument("--workload", choices=("pencil", "batch4096"), default="pencil",
-                    help="pencil: one n x n pencil (the headline); batch4096: 4096 pencils, n ~ U{32..512}")
-    ap.add_argument("--loop-sample", type=int, default=256, help="pencils of the looped baseline (batch workload)")
+    ap.add_argument("--workload", choices=("pencil", "batch4096", "batch256"), default="pencil",
+                    help="pencil: one n x n pencil (the headline); batch4096: 4096 FP64 pencils, n ~ U{32..512}; "
+                         "batch256: 256 pencils, n log-uniform in [256, 4096], 30%% graded, split precision")
+    ap.add_argument("--loop-sample", type=int, default=0,
+                    help="pencils of the looped baseline (batch workloads; 0: the workload's default)")
     ap.add_argument("--n", type=int, default=16000)
     ap.add_argument("--r", type=int, default=16)
     ap.add_argument("--p", type=int, default=4)
@@ -143,6 +145,22 @@ def cpu_oracle_seconds(n_sample: int, r: int, p: int, nq: int, dist: str):
     return time.perf_counter() - t0
 
 
+def cpu_dgghd3_seconds(n_sample: int, dist: str):
+    """Times LAPACK DGGHD3 (the reference driver's one-stage baseline, src/profilereduction.f90:156)
+    once on n_sample with a multithreaded BLAS on all host cores."""
+    from oracle import oracle as O
+    from paraht_gb300.generate import identity, pencil
+
+    O.set_blas_threads(os.cpu_count() or 1)
+    A, B = pencil(n_sample, dist, seed=1302)
+    Q, Z = identity(n_sample), identity(n_sample)
+    t0 = time.perf_counter()
+    O.dgghd3(A, B, Q, Z)
+    dt = time.perf_counter() - t0
+    O.set_blas_threads(1)
+    return dt
+
+
 def run_reference(args, rank: int):
     """--impl reference: the CPU implementation of the path on the host cores."""
     if rank != 0:
@@ -169,48 +187,76 @@ def run_reference(args, rank: int):
     return 0
 
 
-BATCH_METRIC = "batched HT reduction: pencils/s, 4096 pencils n~U{32..512}, FP64"
+BATCHES = {
+    # BASELINE configs: 4096 FP64 pencils n ~ U{32..512}; 256 pencils n log-uniform in [256, 4096],
+    # 70% Std / 30% graded-singular B, split-precision updates
+    "batch4096": dict(count=4096, lo=32, hi=512, law="uniform", graded=0.0, split=False, loop=256,
+                      metric="batched HT reduction: pencils/s, 4096 pencils n~U{32..512}, FP64"),
+    "batch256": dict(count=256, lo=256, hi=4096, law="loguniform", graded=0.3, split=True, loop=12,
+                     metric="batched HT reduction: pencils/s, 256 pencils n log-U[256,4096], 30% graded, split"),
+}
 
 
-def batch_params(n: int):
-    """(r, p, nq) of a batch pencil of size n (the persistent kernel takes p r <= 64)."""
-    return 16, 4, 16
+def batch_params(n: int, split: bool):
+    """(r, p, nq) of a batch pencil of size n from the autotuner's table: the persistent kernel's
+    entry where it takes the pencil (n <= 1024), else the single-pencil path's."""
+    from paraht_gb300 import tune
+
+    if n <= 1024:
+        r, p, nq = tune.pick(n, "batch")
+        if p * r <= 64:
+            return r, p, nq
+    return tune.pick(n, "split" if split else "fp64")
 
 
 def run_batch(args, rank: int, world: int, local: int):
-    """--workload batch4096: 4096 FP64 pencils of uneven size (n ~ U{32..512}, seeded, Std) in one
-    paraht_reduce_batched_d call; the looped single-pencil path on a sample of the same pencils
-    and the CPU oracle on a smaller sample are timed beside it."""
+    """--workload batch4096 / batch256: many pencils of uneven size in one paraht_reduce_batched_d
+    call; the looped single-pencil path on a sample of the same pencils and the CPU oracle on a
+    smaller sample are timed beside it."""
+    import numpy as _np
+
     from paraht_gb300.generate import batch_sizes, identity, pencil
 
-    count, lo, hi = 4096, 32, 512
-    sizes = batch_sizes(count, lo, hi, "uniform", seed=replica_seed(1302, rank))
-    params = [batch_params(n) for n in sizes]
+    spec = BATCHES[args.workload]
+    count, lo, hi = spec["count"], spec["lo"], spec["hi"]
+    sizes = batch_sizes(count, lo, hi, spec["law"], seed=replica_seed(1302, rank))
+    rng = _np.random.default_rng(replica_seed(2604, rank))
+    dists = ["graded" if rng.random() < spec["graded"] else "std" for _ in sizes]
+    params = [batch_params(n, spec["split"]) for n in sizes]
     flops = sum(18.67 * float(n) ** 3 for n in sizes)
-    if args.impl == "reference":
-        if rank != 0:
-            return 0
+    n3 = statistics.mean(float(n) ** 3 for n in sizes)
+    workload = (f"{count} pencils, n {'~U{' + str(lo) + '..' + str(hi) + '}' if spec['law'] == 'uniform' else 'log-U[' + str(lo) + ',' + str(hi) + ']'}"
+                f" (seeded), {int(round(100 * spec['graded']))}% graded, r/p/nq from the autotuner table, "
+                f"{'split-precision single-pencil path above n=1024' if spec['split'] else 'FP64'}, one paraht_reduce_batched_d call")
+
+    def cpu_rate(nsample):
+        """Oracle on the first pencils with n <= 1500, per-pencil time scaled by the batch's mean n^3."""
         from oracle import oracle as O
 
         O.set_blas_threads(1)
-        sample = sizes[:16]
-        ts = []
-        for _ in range(max(1, args.steps)):
+        idx = [i for i, n in enumerate(sizes) if n <= 1500][:nsample]
+        per = []
+        for i in idx:
+            A, B = pencil(sizes[i], dists[i], seed=7 + i)
+            r, p, nq = params[i]
             t0 = time.perf_counter()
-            for i, n in enumerate(sample):
-                A, B = pencil(n, "std", seed=7 + i)
-                r, p, nq = params[i]
-                O.reduce(A, B, identity(n), identity(n), min(r, n), p, min(nq, r))
-            ts.append(time.perf_counter() - t0)
-        v = len(sample) / statistics.mean(ts)
-        cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+            O.reduce(A, B, identity(sizes[i]), identity(sizes[i]), min(r, sizes[i]), p, min(nq, r))
+            per.append((time.perf_counter() - t0) / float(sizes[i]) ** 3)
+        v = 1.0 / (statistics.mean(per) * n3)
+        return v, {"value": v, "unit": "pencils/s", "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)),
+                   "kind": "port", "sample": f"CPU oracle on {len(idx)} pencils of the batch (n <= 1500), one after the "
+                                             f"other, time per pencil scaled by the batch's mean n^3"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        vs = [cpu_rate(4 if spec["split"] else 16) for _ in range(max(1, args.steps))]
+        v = statistics.mean(x[0] for x in vs)
         print(json.dumps({
-            "metric": BATCH_METRIC, "value": v, "unit": "pencils/s", "impl": "reference", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(ts) * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"batch of {count} pencils n~U{{{lo}..{hi}}} Std, r/p/nq=16/4/16"},
-            "cpu_baseline": {"value": v, "unit": "pencils/s", "cores": cores, "kind": "port",
-                             "sample": f"CPU oracle on the first {len(sample)} pencil sizes, one after the other"},
+            "metric": spec["metric"], "value": v, "unit": "pencils/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * count / v, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": workload}, "cpu_baseline": {**vs[-1][1], "value": v},
             "e2e": {"value": v, "unit": "pencils/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}), flush=True)
         return 0
 
@@ -224,7 +270,8 @@ def run_batch(args, rank: int, world: int, local: int):
         import torch.distributed as td
 
         td.init_process_group("nccl", device_id=torch.device("cuda", local))
-    host = [pencil(n, "std", seed=100000 * rank + i) for i, n in enumerate(sizes)]
+    flags = ph.PARAHT_FLAG_SPLIT if spec["split"] else 0
+    host = [pencil(n, d, seed=100000 * rank + i) for i, (n, d) in enumerate(zip(sizes, dists))]
     pris = [[torch.from_numpy(np.ascontiguousarray(X.T)).cuda() for X in ab] for ab in host]
     work = [[torch.empty_like(a), torch.empty_like(a), torch.empty_like(a), torch.empty_like(a)] for a, _ in pris]
     eyes = {}
@@ -241,11 +288,11 @@ def run_batch(args, rank: int, world: int, local: int):
             w[3].copy_(eyes[sizes[i]])
         torch.cuda.synchronize()
 
-    def call(idx, flags):
+    def call(idx, f):
         ns = [sizes[i] for i in idx]
         ptr = lambda j: [work[i][j].data_ptr() for i in idx]  # noqa: E731
         ctx.reduce_batched_d(ns, ptr(0), ns, ptr(1), ns, ptr(2), ns, ptr(3), ns, [params[i][0] for i in idx],
-                             [params[i][1] for i in idx], [params[i][2] for i in idx], flags)
+                             [params[i][1] for i in idx], [params[i][2] for i in idx], f)
 
     def barrier():
         if dist_on:
@@ -256,7 +303,7 @@ def run_batch(args, rank: int, world: int, local: int):
     allidx = list(range(count))
     for _ in range(args.warmup):
         restore(allidx)
-        call(allidx, 0)
+        call(allidx, flags)
     ts, launches = [], 0
     sampler = ClockSampler(local)
     with sampler:
@@ -264,19 +311,28 @@ def run_batch(args, rank: int, world: int, local: int):
             restore(allidx)
             barrier()
             t0 = time.perf_counter()
-            call(allidx, 0)
+            call(allidx, flags)
             ts.append(time.perf_counter() - t0)
             launches += ctx.launch_count()
             barrier()
     t_step = statistics.mean(ts)
     t_step = job_time(t_step, "cuda")
     value = world * count / t_step
+    # backward errors of the last timed call, on the device (FP64 matmuls), every pencil
+    errs = []
+    for i in allidx:
+        A0, B0 = pris[i][0].T, pris[i][1].T
+        H, T, Q, Z = (work[i][j].T for j in range(4))
+        errs.append(max(float(torch.linalg.norm(Q.T @ A0 @ Z - H) / torch.linalg.norm(A0)),
+                        float(torch.linalg.norm(Q.T @ B0 @ Z - T) / torch.linalg.norm(B0))))
+    errs_sorted = sorted(errs)
     # looped baseline: the same call with PARAHT_FLAG_BATCH_LOOP on a sample of the batch
-    sample = allidx[: min(count, args.loop_sample)]
+    sample = allidx[: min(count, args.loop_sample if args.loop_sample > 0 else spec["loop"])]
     restore(sample)
     t0 = time.perf_counter()
-    call(sample, ph.PARAHT_FLAG_BATCH_LOOP)
-    loop_v = len(sample) / (time.perf_counter() - t0)
+    call(sample, flags | ph.PARAHT_FLAG_BATCH_LOOP)
+    t_loop = time.perf_counter() - t0
+    loop_v = 1.0 / (t_loop / sum(float(sizes[i]) ** 3 for i in sample) * n3)  # per-pencil time scaled by n^3
     # end to end: pinned host pencils -> device, batched call, results back (all four matrices)
     hostp = [[torch.from_numpy(np.ascontiguousarray(X.T)).pin_memory() for X in ab] for ab in host]
     outp = [[torch.empty(w[0].shape, dtype=torch.float64).pin_memory() for _ in range(4)] for w in work]
@@ -291,52 +347,35 @@ def run_batch(args, rank: int, world: int, local: int):
         w[3].copy_(eyes[sizes[i]])
         h2d += 2 * w[0].numel() * 8
     torch.cuda.synchronize()
-    call(allidx, 0)
+    call(allidx, flags)
     for i in allidx:
         for j in range(4):
             outp[i][j].copy_(work[i][j], non_blocking=True)
             d2h += work[i][j].numel() * 8
     torch.cuda.synchronize()
     e2e_v = world * count / (time.perf_counter() - t0)
-    # backward error spot check on a few pencils of the last call
-    errs = []
-    for i in allidx[:: max(1, count // 16)]:
-        A0, B0 = (torch.from_numpy(X) for X in host[i])
-        H, T, Q, Z = (torch.from_numpy(outp[i][j].numpy().T) for j in range(4))
-        errs.append(max(float(torch.linalg.norm(Q.T @ A0 @ Z - H) / torch.linalg.norm(A0)),
-                        float(torch.linalg.norm(Q.T @ B0 @ Z - T) / torch.linalg.norm(B0))))
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        from oracle import oracle as O
-
-        O.set_blas_threads(1)
-        cs = sizes[:8]
-        t0 = time.perf_counter()
-        for i, n in enumerate(cs):
-            A, B = pencil(n, "std", seed=7 + i)
-            O.reduce(A, B, identity(n), identity(n), 16, 4, 16)
-        cpu = {"value": len(cs) / (time.perf_counter() - t0), "unit": "pencils/s",
-               "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)), "kind": "port",
-               "sample": f"CPU oracle on the first {len(cs)} pencil sizes of the batch, one after the other"}
+        cpu = cpu_rate(4 if spec["split"] else 8)[1]
     if rank == 0:
         achieved = flops / t_step / 1e12 * world
         print(json.dumps({
-            "metric": BATCH_METRIC, "value": value, "unit": "pencils/s", "n_gpus": world, "steps": args.steps,
+            "metric": spec["metric"], "value": value, "unit": "pencils/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"batch of {count} pencils n~U{{{lo}..{hi}}} (seeded) Std, r/p/nq=16/4/16, FP64, "
-                                   f"one paraht_reduce_batched_d call",
-                       "pencils": count, "n_lo": lo, "n_hi": hi,
-                       "l2": "inputs ~12 GB >> L2; pristine inputs restored between steps outside the timed region"},
+            "config": {"workload": workload, "pencils": count, "n_lo": lo, "n_hi": hi, "size_law": spec["law"],
+                       "graded_fraction": spec["graded"], "split": spec["split"],
+                       "l2": "inputs >> L2; pristine inputs restored between steps outside the timed region"},
             "e2e": {"value": e2e_v, "unit": "pencils/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
             "looped_baseline": {"value": loop_v, "unit": "pencils/s", "sample": len(sample),
+                                "note": "paraht_reduce_d per pencil, time per pencil scaled to the batch's mean n^3",
                                 "speedup": value / world / loop_v},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": 1.19, "unit": "TFLOP/s",
                          "frac": achieved / 1.19, "traffic": None,
-                         "kernel": "k_batch_reduce (nominal 18.67 n^3 flops per pencil)",
+                         "kernel": "k_batch_reduce and the single-pencil kernels (nominal 18.67 n^3 flops per pencil)",
                          "peak_source": "FP64 FMA throughput measured on this pool's GB300 (fp64 probe)"},
-            "max_bwd_err_sampled": max(errs),
+            "bwd_err": {"max": errs_sorted[-1], "p99": errs_sorted[min(len(errs) - 1, int(0.99 * len(errs)))]},
             "cpu_baseline": cpu,
             "clocks": sampler.summary(),
         }), flush=True)
@@ -495,7 +534,7 @@ def main():
                     "traffic": None, "kernel": "k_apply_left/k_apply_right (FP64 compact-WY op lists)",
                     "peak_source": "FP64 FMA throughput measured on this pool's GB300 (fp64 probe)"}
 
-    cpu = None
+    cpu = cpu_dgghd3 = None
     if rank == 0 and not args.no_cpu_baseline:
         ns = args.cpu_sample_n
         ts = cpu_oracle_seconds(ns, r, p, nq, args.dist)
@@ -503,6 +542,9 @@ def main():
                                                                                         os.cpu_count() or 1)),
                "kind": "port",
                "sample": f"CPU oracle (OpenMP restatement of the reference) at n={ns}: {ts:.2f} s, scaled by (n/{ns})^3"}
+        td3 = cpu_dgghd3_seconds(ns, args.dist)
+        cpu_dgghd3 = {"value": td3 * (n / ns) ** 3, "unit": "s", "cores": os.cpu_count() or 1,
+                      "sample": f"LAPACK DGGHD3 (scipy's OpenBLAS, all cores) at n={ns}: {td3:.2f} s, scaled by (n/{ns})^3"}
 
     if rank == 0:
         line = {
@@ -520,6 +562,7 @@ def main():
             "effective_gflops": flops_nominal(n) / t_step / 1e9,
             "roofline": roofline,
             "cpu_baseline": cpu,
+            "cpu_dgghd3": cpu_dgghd3,
             "clocks": sampler.summary(),
         }
         if check:

@@ -136,6 +136,20 @@ int paraht_reduce_batched_d(paraht_ctx ctx, int count, const int* n, double* con
                             double* const* B, const int* ldb, double* const* Q, const int* ldq, double* const* Z,
                             const int* ldz, const int* r, const int* p, const int* nq, int flags);
 
+/* ---- LAPACK DGGHD3-compatible entry (no counterpart in the reference, which ignores ilo/ihi;
+ * the argument list of dgghd3 as the reference driver calls it, src/profilereduction.f90:156,
+ * without the work array): reduces rows/columns ilo..ihi (1-based) of the pencil, A and B
+ * assumed upper triangular outside them as after balancing, by the two-stage reduction with
+ * (r, p, nq), and applies the transformations to the rest of A and B.
+ * compq/compz: 'N' Q/Z not referenced, 'I' Q/Z set to the identity first, 'V' Q/Z right-multiplied
+ * (accumulated, as the reference does).  Status: LAPACK-style -i for the i-th argument
+ * (1 compq .. 13 ldz, 14 r, 15 p, 16 nq), else as paraht_reduce_d.  _d: device pointers on ctx;
+ * the plain form takes host arrays. ---- */
+int paraht_gghd3_d(paraht_ctx ctx, char compq, char compz, int n, int ilo, int ihi, double* A, int lda, double* B,
+                   int ldb, double* Q, int ldq, double* Z, int ldz, int r, int p, int nq, int flags);
+int paraht_gghd3(char compq, char compz, int n, int ilo, int ihi, double* A, int lda, double* B, int ldb, double* Q,
+                 int ldq, double* Z, int ldz, int r, int p, int nq, int flags);
+
 /* ---- misc ---- */
 const char* paraht_strerror(int status);
 int paraht_version(void);

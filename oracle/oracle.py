@@ -33,6 +33,7 @@ def lib():
         L.oracle_rht2ht_householder.argtypes = [i, d, i, d, i, d, i, d, i, i, i, i, d]
         L.oracle_rht2ht_unblocked.argtypes = [i, d, i, d, i, d, i, d, i, i]
         L.oracle_dgghd3.argtypes = [i, d, i, d, i, d, i, d, i]
+        L.oracle_dgghd3_range.argtypes = [C.c_char, C.c_char, i, i, i, d, i, d, i, d, i, d, i]
         L.oracle_dhgeqz_eigs.argtypes = [i, d, i, d, i, d, d, d]
         L.oracle_triangularize.argtypes = [i, d, i]
         L.oracle_backward_error.argtypes = [i, d, i, d, i, d, i, d, i]
@@ -97,6 +98,14 @@ def dgghd3(A, B, Q, Z):
     _check(A, B, Q, Z)
     n = A.shape[0]
     return lib().oracle_dgghd3(n, _ptr(A), n, _ptr(B), n, _ptr(Q), n, _ptr(Z), n)
+
+
+def dgghd3_range(compq, compz, ilo, ihi, A, B, Q, Z):
+    """LAPACK dgghd3(compq, compz, n, ilo, ihi, ...) in place (1-based ilo/ihi)."""
+    _check(A, B, Q, Z)
+    n = A.shape[0]
+    return lib().oracle_dgghd3_range(compq.encode(), compz.encode(), n, int(ilo), int(ihi), _ptr(A), n, _ptr(B), n,
+                                     _ptr(Q), n, _ptr(Z), n)
 
 
 def dhgeqz_eigs(H, T):

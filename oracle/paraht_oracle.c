@@ -845,6 +845,23 @@ int oracle_dgghd3(int n, double* A, int lda, double* B, int ldb, double* Q, int 
   return info;
 }
 
+/* dgghd3 with the caller's compq/compz and ilo/ihi (LAPACK's own interface), the checker of the
+ * library's DGGHD3-compatible entry. */
+int oracle_dgghd3_range(char compq, char compz, int n, int ilo, int ihi, double* A, int lda, double* B, int ldb,
+                        double* Q, int ldq, double* Z, int ldz) {
+  if (init_lapack()) return -100;
+  lint nn = n, lo = ilo, hi = ihi, info = 0, lwork = -1;
+  lint la = lda, lb = ldb, lq = ldq, lz = ldz;
+  char cq[2] = {compq, 0}, cz[2] = {compz, 0};
+  double q;
+  LP->dgghd3(cq, cz, &nn, &lo, &hi, A, &la, B, &lb, Q, &lq, Z, &lz, &q, &lwork, &info, 1, 1);
+  lwork = MAX((lint)q, 1);
+  double* work = malloc(sizeof(double) * lwork);
+  LP->dgghd3(cq, cz, &nn, &lo, &hi, A, &la, B, &lb, Q, &lq, Z, &lz, work, &lwork, &info, 1, 1);
+  free(work);
+  return info;
+}
+
 /* Generalized eigenvalues of an HT pencil via DHGEQZ('E','N','N') (no Schur vectors). */
 int oracle_dhgeqz_eigs(int n, double* H, int ldh, double* T, int ldt, double* alphar, double* alphai, double* beta) {
   if (init_lapack()) return -100;

@@ -27,7 +27,7 @@ from ._lib import (PARAHT_BATCH_MAX_N, PARAHT_FLAG_BATCH_LOOP, PARAHT_FLAG_CHECK
                    ParahtError, check, lib)
 
 __all__ = [
-    "ab2rht_simple", "rht2ht_householder", "reduce", "Context", "ParahtError",
+    "ab2rht_simple", "rht2ht_householder", "reduce", "gghd3", "Context", "ParahtError",
     "PARAHT_FLAG_TIME_COMPONENTS", "PARAHT_FLAG_CHECK_FINITE", "PARAHT_FLAG_SPLIT", "PARAHT_FLAG_NO_ZERO_FILL",
     "PARAHT_FLAG_SEQUENTIAL", "PARAHT_FLAG_KERNEL_TIMES", "PARAHT_FLAG_BATCH_LOOP", "PARAHT_BATCH_MAX_N",
 ]
@@ -63,6 +63,17 @@ def reduce(A, B, Q, Z, r, p, nq, flags=0):
     n = A.shape[0]
     check(lib().paraht_reduce(int(n), _host_ptr(A), A.shape[0], _host_ptr(B), B.shape[0], _host_ptr(Q), Q.shape[0],
                               _host_ptr(Z), Z.shape[0], int(r), int(p), int(nq), int(flags)), "reduce")
+
+
+def gghd3(compq, compz, ilo, ihi, A, B, Q, Z, r=16, p=4, nq=16, flags=0):
+    """LAPACK DGGHD3-compatible reduction of rows/columns ilo..ihi (1-based) on host arrays, in
+    place: compq/compz 'N' (Q/Z not referenced, may be None), 'I' (identity first) or 'V'
+    (accumulated).  No counterpart in the reference (which ignores ilo/ihi)."""
+    n = A.shape[0]
+    check(lib().paraht_gghd3(compq.encode(), compz.encode(), int(n), int(ilo), int(ihi), _host_ptr(A), A.shape[0],
+                             _host_ptr(B), B.shape[0], _host_ptr(Q), Q.shape[0] if Q is not None else 1,
+                             _host_ptr(Z), Z.shape[0] if Z is not None else 1, int(r), int(p), int(nq), int(flags)),
+          "gghd3")
 
 
 class Context:

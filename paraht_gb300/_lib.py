@@ -52,6 +52,8 @@ SIGNATURES = {
     "paraht_reduce_batched_d": [C.c_void_p, _i, C.POINTER(_i), C.POINTER(_d), C.POINTER(_i), C.POINTER(_d),
                                 C.POINTER(_i), C.POINTER(_d), C.POINTER(_i), C.POINTER(_d), C.POINTER(_i),
                                 C.POINTER(_i), C.POINTER(_i), C.POINTER(_i), _i],
+    "paraht_gghd3": [C.c_char, C.c_char, _i, _i, _i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i, _i, _i],
+    "paraht_gghd3_d": [C.c_void_p, C.c_char, C.c_char, _i, _i, _i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i, _i, _i],
     "paraht_strerror": [_i],
     "paraht_version": [],
 }

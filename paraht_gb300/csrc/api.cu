@@ -4,8 +4,11 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cctype>
+#include <atomic>
 #include <mutex>
 #include <new>
+#include <thread>
 
 #include "launch_count.h"
 #include "paraht_impl.h"
@@ -218,6 +221,9 @@ extern "C" int paraht_ctx_destroy(paraht_ctx c) {
     cudaStreamSynchronize(x.bstream);
     cudaStreamDestroy(x.bstream);
   }
+  for (void* w : x.workers) paraht_ctx_destroy((paraht_ctx)w);
+  x.workers.clear();
+  if (x.gws) cudaFree(x.gws);
   if (x.bws) cudaFree(x.bws);
   if (x.ev_a) cudaEventDestroy(x.ev_a);
   if (x.ev_b) cudaEventDestroy(x.ev_b);
@@ -623,10 +629,49 @@ extern "C" int paraht_reduce_batched_d(paraht_ctx c, int count, const int* n, do
       launches += pht::tl_launches - l0;
     }
   }
-  for (int i : large) {  // overlapping the persistent launch
-    if (rc) break;
-    rc = run_device(x, 3, n[i], A[i], lda[i], B[i], ldb[i], Q[i], ldq[i], Z[i], ldz[i], r[i], p[i], nq[i], single_flags);
-    launches += x.launches;
+  // the other pencils through the single-pencil path, overlapping the persistent launch: several
+  // at once on worker contexts (own streams and workspace, one host thread each), since one
+  // pencil's serial chains leave most SMs idle
+  const int nworkers = std::min<int>(pht::kBatchWorkers, (int)large.size());
+  if (!rc && nworkers <= 1) {
+    for (int i : large) {
+      rc = run_device(x, 3, n[i], A[i], lda[i], B[i], ldb[i], Q[i], ldq[i], Z[i], ldz[i], r[i], p[i], nq[i],
+                      single_flags);
+      if (rc) break;
+      launches += x.launches;
+    }
+  } else if (!rc) {
+    while ((int)x.workers.size() < nworkers && !rc) {
+      paraht_ctx w = nullptr;
+      rc = paraht_ctx_create(&w, x.device);
+      if (!rc) x.workers.push_back(w);
+    }
+    if (!rc) {
+      cudaEventRecord(x.ev_b, x.stream);  // the pencils may have been produced on this stream
+      for (int k = 0; k < nworkers; ++k) cudaStreamWaitEvent(((paraht_ctx)x.workers[k])->c.stream, x.ev_b, 0);
+      std::atomic<int> next(0), err(0);
+      std::atomic<long long> wl(0);
+      std::vector<std::thread> th;
+      for (int k = 0; k < nworkers; ++k)
+        th.emplace_back([&, k]() {
+          Ctx& wx = ((paraht_ctx)x.workers[k])->c;
+          cudaSetDevice(wx.device);
+          for (int j = next++; j < (int)large.size() && err.load() == 0; j = next++) {
+            const int i = large[j];
+            int e = run_device(wx, 3, n[i], A[i], lda[i], B[i], ldb[i], Q[i], ldq[i], Z[i], ldz[i], r[i], p[i], nq[i],
+                               single_flags);
+            if (!e) e = finish(wx);
+            wl += wx.launches;
+            if (e) {
+              int zero = 0;
+              err.compare_exchange_strong(zero, e);
+            }
+          }
+        });
+      for (auto& h : th) h.join();
+      rc = err.load();
+      launches += wl.load();
+    }
   }
   if (!small.empty() && x.bstream) {
     const cudaError_t e = cudaStreamSynchronize(x.bstream);
@@ -634,6 +679,148 @@ extern "C" int paraht_reduce_batched_d(paraht_ctx c, int count, const int* n, do
   }
   if (!rc) rc = finish(x);
   x.launches = launches;
+  cudaSetDevice(prev);
+  return rc;
+}
+
+// ---- DGGHD3-compatible entry ----
+static int gghd3_check(char compq, char compz, int n, int ilo, int ihi, const double* A, int lda, const double* B,
+                       int ldb, const double* Q, int ldq, const double* Z, int ldz, int r, int p, int nq) {
+  auto ok = [](char c) { return c == 'N' || c == 'I' || c == 'V' || c == 'n' || c == 'i' || c == 'v'; };
+  if (!ok(compq)) return -1;
+  if (!ok(compz)) return -2;
+  if (n < 0) return -3;
+  if (ilo < 1) return -4;
+  if (ihi > n || ihi < ilo - 1) return -5;
+  const int ldmin = std::max(1, n);
+  if (n > 0 && !A) return -6;
+  if (lda < ldmin) return -7;
+  if (n > 0 && !B) return -8;
+  if (ldb < ldmin) return -9;
+  const bool wq = compq != 'N' && compq != 'n', wz = compz != 'N' && compz != 'n';
+  if (wq && n > 0 && !Q) return -10;
+  if ((wq && ldq < ldmin) || ldq < 1) return -11;
+  if (wz && n > 0 && !Z) return -12;
+  if ((wz && ldz < ldmin) || ldz < 1) return -13;
+  if (r < 1 || r > 64) return -14;
+  if (p < 2) return -15;
+  if (nq < 1 || nq > r) return -16;
+  return 0;
+}
+
+// On x's stream; A, B, Q, Z device pointers (Q/Z may be null when not referenced).
+static int gghd3_device(Ctx& x, char compq, char compz, int n, int ilo, int ihi, double* A, int lda, double* B,
+                        int ldb, double* Q, int ldq, double* Z, int ldz, int r, int p, int nq, int flags) {
+  const char cq = (char)toupper(compq), cz = (char)toupper(compz);
+  const long long l0 = pht::tl_launches;
+  if (cq == 'I') pht::set_identity(x.stream, n, Q, ldq);
+  if (cz == 'I') pht::set_identity(x.stream, n, Z, ldz);
+  const int m = ihi - ilo + 1;
+  int rc = 0;
+  if (m >= 2) {
+    // Q_s, Z_s (m x m) and one GEMM output of at most n x m
+    const size_t need = sizeof(double) * (2 * (size_t)m * m + (size_t)std::max(n, 1) * m);
+    if (need > x.gws_bytes) {
+      if (x.gws) cudaFree(x.gws);
+      x.gws = nullptr;
+      x.gws_bytes = 0;
+      if (cudaMalloc(&x.gws, need) != cudaSuccess) {
+        cudaGetLastError();
+        return PARAHT_ERR_ALLOC;
+      }
+      x.gws_bytes = need;
+    }
+    double* Qs = x.gws;
+    double* Zs = Qs + (size_t)m * m;
+    double* Tm = Zs + (size_t)m * m;
+    pht::set_identity(x.stream, m, Qs, m);
+    pht::set_identity(x.stream, m, Zs, m);
+    const size_t o = (size_t)(ilo - 1);
+    rc = run_device(x, 3, m, A + o + o * lda, lda, B + o + o * ldb, ldb, Qs, m, Zs, m, r, p, nq,
+                    flags & ~(PARAHT_FLAG_TIME_COMPONENTS | PARAHT_FLAG_KERNEL_TIMES));
+    if (!rc) {
+      auto copy_back = [&](double* dst, int ldd, int rows, int cols) {
+        cudaMemcpy2DAsync(dst, (size_t)ldd * sizeof(double), Tm, (size_t)rows * sizeof(double),
+                          (size_t)rows * sizeof(double), cols, cudaMemcpyDeviceToDevice, x.stream);
+      };
+      double* M2[2] = {A, B};
+      const int ld2[2] = {lda, ldb};
+      for (int k = 0; k < 2; ++k) {
+        if (ilo > 1) {  // rows above the block: X(1:ilo-1, ilo:ihi) <- X(1:ilo-1, ilo:ihi) Z_s
+          double* top = M2[k] + o * ld2[k];
+          pht::dgemm(x.stream, false, ilo - 1, m, m, top, ld2[k], Zs, m, Tm, ilo - 1);
+          copy_back(top, ld2[k], ilo - 1, m);
+        }
+        if (ihi < n) {  // columns right of the block: X(ilo:ihi, ihi+1:n) <- Q_s^T X(ilo:ihi, ihi+1:n)
+          double* right = M2[k] + o + (size_t)ihi * ld2[k];
+          pht::dgemm(x.stream, true, m, n - ihi, m, Qs, m, right, ld2[k], Tm, m);
+          copy_back(right, ld2[k], m, n - ihi);
+        }
+      }
+      if (cq != 'N') {  // Q(:, ilo:ihi) <- Q(:, ilo:ihi) Q_s
+        double* blk = Q + o * ldq;
+        pht::dgemm(x.stream, false, n, m, m, blk, ldq, Qs, m, Tm, n);
+        copy_back(blk, ldq, n, m);
+      }
+      if (cz != 'N') {
+        double* blk = Z + o * ldz;
+        pht::dgemm(x.stream, false, n, m, m, blk, ldz, Zs, m, Tm, n);
+        copy_back(blk, ldz, n, m);
+      }
+    }
+  }
+  if (!rc) rc = finish(x);
+  x.launches = pht::tl_launches - l0;
+  return rc;
+}
+
+extern "C" int paraht_gghd3_d(paraht_ctx c, char compq, char compz, int n, int ilo, int ihi, double* A, int lda,
+                              double* B, int ldb, double* Q, int ldq, double* Z, int ldz, int r, int p, int nq,
+                              int flags) {
+  if (!ctx_ok(c)) return PARAHT_ERR_BAD_CTX;
+  int rc = gghd3_check(compq, compz, n, ilo, ihi, A, lda, B, ldb, Q, ldq, Z, ldz, r, p, nq);
+  if (rc || n == 0) return rc;
+  Ctx& x = c->c;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(x.device);
+  rc = gghd3_device(x, compq, compz, n, ilo, ihi, A, lda, B, ldb, Q, ldq, Z, ldz, r, p, nq, flags);
+  cudaSetDevice(prev);
+  return rc;
+}
+
+extern "C" int paraht_gghd3(char compq, char compz, int n, int ilo, int ihi, double* A, int lda, double* B, int ldb,
+                            double* Q, int ldq, double* Z, int ldz, int r, int p, int nq, int flags) {
+  int rc = gghd3_check(compq, compz, n, ilo, ihi, A, lda, B, ldb, Q, ldq, Z, ldz, r, p, nq);
+  if (rc || n == 0) return rc;
+  paraht_ctx c;
+  rc = default_ctx(&c);
+  if (rc) return rc;
+  Ctx& x = c->c;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(x.device);
+  const int ldd = (n + 3) & ~3;
+  rc = x.ensure_staging((size_t)ldd * n * sizeof(double));
+  if (!rc) {
+    const bool wq = toupper(compq) != 'N', wz = toupper(compz) != 'N';
+    double* h[4] = {A, B, Q, Z};
+    const int ld[4] = {lda, ldb, ldq, ldz};
+    const bool use[4] = {true, true, wq, wz};
+    for (int i = 0; i < 4; ++i)
+      if (use[i] && !(i >= 2 && toupper(i == 2 ? compq : compz) == 'I'))
+        cudaMemcpy2DAsync(x.stage[i], (size_t)ldd * sizeof(double), h[i], (size_t)ld[i] * sizeof(double),
+                          (size_t)n * sizeof(double), n, cudaMemcpyHostToDevice, x.stream);
+    rc = gghd3_device(x, compq, compz, n, ilo, ihi, x.stage[0], ldd, x.stage[1], ldd, wq ? x.stage[2] : nullptr, ldd,
+                      wz ? x.stage[3] : nullptr, ldd, r, p, nq, flags);
+    if (!rc)
+      for (int i = 0; i < 4; ++i)
+        if (use[i])
+          cudaMemcpy2DAsync(h[i], (size_t)ld[i] * sizeof(double), x.stage[i], (size_t)ldd * sizeof(double),
+                            (size_t)n * sizeof(double), n, cudaMemcpyDeviceToHost, x.stream);
+    const int rc2 = finish(x);
+    if (!rc) rc = rc2;
+  }
   cudaSetDevice(prev);
   return rc;
 }

@@ -92,7 +92,13 @@ struct Ctx {
   size_t bws_bytes = 0;
   std::vector<char> bhost;
   cudaStream_t bstream = nullptr;
+  // worker contexts (paraht_ctx handles) reducing the batch's other pencils concurrently
+  std::vector<void*> workers;
+  // DGGHD3-compatible entry: Q_s, Z_s of the diagonal block and the GEMM output buffer
+  double* gws = nullptr;
+  size_t gws_bytes = 0;
 };
+constexpr int kBatchWorkers = 4;
 
 size_t s1_workspace_bytes(int n, int nb, int p);
 size_t s2_workspace_bytes(int n, int r, int nq);
@@ -104,6 +110,10 @@ int s2_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
 // largest absolute value zeroed in dres[0] (A) and dres[1] (B).
 void zero_fill(cudaStream_t s, int n, double* A, int lda, int band, double* B, int ldb, double* dres);
 int check_finite(cudaStream_t s, int n, const double* A, int lda, const double* B, int ldb, int* dflag);
+// FP64 GEMM Out = op(X) Y (op = transpose when tx) and identity fill (gemm.cu).
+void dgemm(cudaStream_t s, bool tx, int M, int N, int K, const double* X, int ldx, const double* Y, int ldy,
+           double* Out, int ldo);
+void set_identity(cudaStream_t s, int n, double* X, int ldx);
 // Batched reduction (batched.cu): which pencils the persistent kernel takes, and one launch
 // over the pencils idx[] of the batch on stream s.
 bool batch_eligible(int n, int r, int p, int nq);

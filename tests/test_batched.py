@@ -16,8 +16,8 @@ from paraht_gb300.generate import identity
 
 pytestmark = pytest.mark.gpu
 
-# n, r, p, nq, dist: persistent-kernel pencils of several shapes, edge sizes, one graded pencil,
-# and one the kernel does not take (p r = 128)
+# n, r, p, nq, dist: persistent-kernel pencils of several shapes, edge sizes, graded pencils,
+# and three the kernel does not take (p r = 128), which run concurrently on worker contexts
 CASES = [
     (1, 2, 2, 2, "std"),
     (3, 2, 2, 2, "std"),
@@ -29,6 +29,8 @@ CASES = [
     (257, 16, 4, 16, "std"),
     (64, 32, 2, 16, "std"),
     (150, 32, 4, 16, "std"),
+    (120, 32, 4, 8, "std"),
+    (90, 16, 8, 16, "graded"),
 ]
 
 
