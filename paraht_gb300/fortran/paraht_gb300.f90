@@ -14,7 +14,7 @@
 !   gfortran ... your_program.f90 paraht_gb300.o -L<dir of libparaht.so> -lparaht -Wl,-rpath,<dir>
 
 module paraht_c
-   use iso_c_binding, only: c_int, c_double
+   use iso_c_binding, only: c_int, c_double, c_char
    implicit none
    interface
       integer(c_int) function paraht_ab2rht(n, A, lda, B, ldb, Q, ldq, Z, ldz, nb, p, time_components) &
@@ -37,6 +37,15 @@ module paraht_c
          integer(c_int), value :: n, lda, ldb, ldq, ldz, r, p, nq, flags
          real(c_double) :: A(*), B(*), Q(*), Z(*)
       end function paraht_reduce
+
+      ! LAPACK DGGHD3's arguments (without the work array) plus r, p, nq, flags
+      integer(c_int) function paraht_gghd3(compq, compz, n, ilo, ihi, A, lda, B, ldb, Q, ldq, Z, ldz, &
+                                           r, p, nq, flags) bind(C, name="paraht_gghd3")
+         import :: c_int, c_double, c_char
+         character(kind=c_char), value :: compq, compz
+         integer(c_int), value :: n, ilo, ihi, lda, ldb, ldq, ldz, r, p, nq, flags
+         real(c_double) :: A(*), B(*), Q(*), Z(*)
+      end function paraht_gghd3
    end interface
 
 contains

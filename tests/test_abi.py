@@ -86,3 +86,29 @@ def test_python_wrapper_raises_with_argument_index():
     assert e.value.status == -11
     with pytest.raises(TypeError):
         ph.ab2rht_simple(n, np.zeros((n, n)), n, A, n, A, n, A, n, 4, 2, False)  # C order rejected
+
+
+@pytest.mark.parametrize("args,expected", [
+    ((b"X", b"I", 10, 1, 10), -1),   # compq
+    ((b"I", b"?", 10, 1, 10), -2),   # compz
+    ((b"I", b"I", -1, 1, 10), -3),   # n
+    ((b"I", b"I", 10, 0, 10), -4),   # ilo < 1
+    ((b"I", b"I", 10, 5, 3), -5),    # ihi < ilo - 1
+    ((b"I", b"I", 10, 1, 11), -5),   # ihi > n
+])
+def test_gghd3_argument_errors_before_any_gpu_work(args, expected):
+    A = np.zeros((10, 10), order="F")
+    p = A.ctypes.data
+    rc = _lib.lib().paraht_gghd3(*args, p, 10, p, 10, p, 10, p, 10, 4, 2, 2, 0)
+    assert rc == expected
+
+
+def test_gghd3_leading_dimension_and_parameter_errors():
+    A = np.zeros((10, 10), order="F")
+    p = A.ctypes.data
+    L = _lib.lib()
+    assert L.paraht_gghd3(b"I", b"I", 10, 1, 10, p, 9, p, 10, p, 10, p, 10, 4, 2, 2, 0) == -7
+    assert L.paraht_gghd3(b"N", b"I", 10, 1, 10, p, 10, p, 10, None, 1, p, 10, 4, 2, 2, 0) != -11  # Q unused
+    assert L.paraht_gghd3(b"V", b"I", 10, 1, 10, p, 10, p, 10, p, 5, p, 10, 4, 2, 2, 0) == -11
+    assert L.paraht_gghd3(b"I", b"I", 10, 1, 10, p, 10, p, 10, p, 10, p, 10, 4, 1, 2, 0) == -15
+    assert L.paraht_gghd3(b"I", b"I", 10, 1, 10, p, 10, p, 10, p, 10, p, 10, 4, 2, 5, 0) == -16
