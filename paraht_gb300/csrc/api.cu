@@ -612,6 +612,8 @@ extern "C" int paraht_reduce_batched_d(paraht_ctx c, int count, const int* n, do
                             pht::batch_eligible(n[i], r[i], p[i], nq[i]);
     (persistent ? small : large).push_back(i);
   }
+  // the single-pencil path takes the largest pencils first (its workers finish together)
+  std::stable_sort(large.begin(), large.end(), [&](int a, int b) { return n[a] > n[b]; });
   int rc = 0;
   long long launches = 0;
   if (!small.empty()) {

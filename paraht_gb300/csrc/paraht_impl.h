@@ -98,7 +98,7 @@ struct Ctx {
   double* gws = nullptr;
   size_t gws_bytes = 0;
 };
-constexpr int kBatchWorkers = 4;
+constexpr int kBatchWorkers = 8;
 
 size_t s1_workspace_bytes(int n, int nb, int p);
 size_t s2_workspace_bytes(int n, int r, int nq);

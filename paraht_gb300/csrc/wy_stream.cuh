@@ -8,21 +8,23 @@
 // writing it back when it leaves the window or the list ends.
 //
 // Number format.  A resident row is held in fixed point, int64 values v with x = v 2^(e-62) for
-// a per-row scale e.  Each op is orthogonal, so a row's values never exceed the 2-norm of all
-// values the row has held; e is set 9 bits above the largest magnitude loaded (enough for
-// 2^18 columns) and raised (all resident values shifted) when a larger value is loaded.  The
-// spacing 2^(e-62) is about 2^-53 of the row's largest element, the resolution of FP64.
+// a per-row scale e, set 5 bits above the largest magnitude loaded (|v| < 2^57) and raised (all
+// resident values shifted) when a larger value is loaded.  Each op is orthogonal on its span, so
+// its results are bounded by the 2-norm of its inputs, at most 8 (= sqrt(64)) times their
+// largest value; before every op a row whose largest value among the op's columns has reached
+// 2^58 is shifted down to below 2^57, so no value ever reaches 2^62.  The spacing 2^(e-62) is
+// 2^-56 of the row's largest loaded element, finer than FP64's 2^-53 at that magnitude.
 //
 // Products.  Each op is two exact digit products on the tensor cores (mma.sync m16n8k16,
 // FP16 inputs, FP32 accumulation), X = C V and C -= X W with W = T V^T formed once per op, or
 // three, X = C V, Y = X T, C -= Y V^T, for lists that mask Y (below).  Operands are split into
 // 8 digits of 7 bits (x = 2^e sum_t d_t 2^{-7(t+1)}, |d_t| <= 128, one power-of-two scale per
-// row of the left and per column of the right factor, the Ozaki scheme); the 36 digit pairs
-// with t+u <= 7 are accumulated per level l = t+u exactly in FP32 over at most 32 inner terms
+// row of the left and per column of the right factor, the Ozaki scheme); the 43 digit pairs
+// with t+u <= 8 are accumulated per level l = t+u exactly in FP32 over at most 32 inner terms
 // (|a_l| < 2^22), in accumulators biased by 1.5 2^23 so that each level is read off the FP32
-// bit pattern with one integer subtraction, and recombined exactly in int64/int128.  Each
-// product is as accurate as an FP64 dot product (the omitted levels are below 2^-56 of row
-// scale x column scale).  X and Y are rounded to 56-bit digits before the next product; C's
+// bit pattern with one integer subtraction, and recombined exactly in int64/int128.  The
+// omitted levels (t+u >= 9) are below 2^-60 of row scale x column scale per inner term, so an
+// element much smaller than its row's largest still gets about FP64 accuracy.  X and Y are rounded to 56-bit digits before the next product; C's
 // correction is added in integer arithmetic.  There is no FP64 instruction in the op loop
 // (on GB300 each FP64 warp instruction occupies a scheduler's FP64 pipe for about 64 cycles).
 // The digits of C, X and Y are formed in registers, directly in the MMA fragment layout.
@@ -49,7 +51,7 @@
 namespace pht {
 
 constexpr int kWsD = 8;            // digits per operand (7 bits each)
-constexpr int kWsLv = 8;           // levels kept (t + u <= 7)
+constexpr int kWsLv = 9;           // levels kept (t + u <= 8)
 constexpr int kWsK = 16;           // reflectors per op
 constexpr int kWsLen = 64;         // span per op
 constexpr int kWsWarps = 4;        // 16 strip rows per warp
@@ -60,7 +62,8 @@ constexpr int kWsPL = kWsLen + 8;  // fp16 pitch of len-indexed digit rows (conf
 constexpr int kWsPK = kWsK + 8;    // fp16 pitch of k-indexed digit rows
 constexpr int kWsMM = 32;          // largest span with the one-product form C -= C M
 constexpr int kWsPM = kWsMM + 8;   // fp16 pitch of M's digit rows
-constexpr int kWsHead = 9;         // headroom bits of the row scale
+constexpr int kWsHead = 5;         // headroom bits of the row scale at load time
+constexpr int kWsGuard = 57;       // a row is shifted down before an op when a value passes 2^57
 constexpr int kWsNoScale = -2000;  // row scale not set yet (no nonzero value loaded)
 
 // Operand digits of one op, prepared once per op (k_ws_prep) and copied to shared memory.  In the
@@ -158,15 +161,16 @@ PHT_DEV uint16_t ws_h1(uint32_t d, bool neg) { return (uint16_t)ws_h2(d, 0, neg,
 constexpr float kWsMagic = 12582912.0f;
 PHT_DEV int ws_lv(float f) { return __float_as_int(f) - 0x4B400000; }
 
-// sum_l a_l 2^{-7l} = 2^{-21} Nh + 2^{-49} Nl, accumulated exactly; a_l read from the biased
-// accumulators (|a_l| <= 8 pairs x 32 terms x 128 x 127 < 2^22)
+// sum_l a_l 2^{-7l} = 2^{-21} Nh + 2^{-56} Nl (levels 0-3 in Nh, 4-8 in Nl), accumulated exactly;
+// a_l read from the biased accumulators (|a_l| <= 8 pairs x 32 terms x 128 x 127 < 2^22)
 PHT_DEV void ws_add_levels(const float* a, long long& Nh, long long& Nl) {
   Nh += ((long long)ws_lv(a[0]) << 21) + ((long long)ws_lv(a[1]) << 14) + ((long long)ws_lv(a[2]) << 7) + ws_lv(a[3]);
-  Nl += ((long long)ws_lv(a[4]) << 21) + ((long long)ws_lv(a[5]) << 14) + ((long long)ws_lv(a[6]) << 7) + ws_lv(a[7]);
+  Nl += ((long long)ws_lv(a[4]) << 28) + ((long long)ws_lv(a[5]) << 21) + ((long long)ws_lv(a[6]) << 14) +
+        ((long long)ws_lv(a[7]) << 7) + ws_lv(a[8]);
 }
 
-// (Nh 2^28 + Nl) as a signed 128-bit integer: the product is 2^(e_left + e_right - 63) times it
-PHT_DEV __int128 ws_join(long long Nh, long long Nl) { return ((__int128)Nh << 28) + (__int128)Nl; }
+// (Nh 2^35 + Nl) as a signed 128-bit integer: the product is 2^(e_left + e_right - 70) times it
+PHT_DEV __int128 ws_join(long long Nh, long long Nl) { return ((__int128)Nh << 35) + (__int128)Nl; }
 
 PHT_DEV void ws_mma(float* c, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0, uint32_t b1) {
   asm volatile(
@@ -574,6 +578,33 @@ __global__ void __launch_bounds__(kWsThreads, kOne ? 3 : 2)
       mA = max(mA, (uint64_t)__shfl_xor_sync(0xffffffffu, (long long)mA, 2));
       mB = max(mB, (uint64_t)__shfl_xor_sync(0xffffffffu, (long long)mB, 1));
       mB = max(mB, (uint64_t)__shfl_xor_sync(0xffffffffu, (long long)mB, 2));
+      // growth guard: shift a row down (raise its scale) when its largest value among the op's
+      // columns has more than kWsGuard bits, so that the op's results stay below 2^62
+      int shA = 0, shB = 0;
+      if (mA >> kWsGuard) shA = (64 - __clzll((long long)mA)) - kWsGuard;
+      if (mB >> kWsGuard) shB = (64 - __clzll((long long)mB)) - kWsGuard;
+      if (__any_sync(0xffffffffu, shA || shB)) {
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh) {
+          const int sh = hh ? shB : shA, rr = hh ? rB : rA;
+          const int rowl = gq + 8 * hh;
+          if (!sh || rowl >= nrows) continue;
+          for (int q = tq; q < kWsCW; q += 4) {
+            if (W.tag[q] < 0) continue;
+            const long long v = S.win[rr][q];
+            const uint64_t a = ws_scale64((uint64_t)(v < 0 ? -v : v), -sh);
+            S.win[rr][q] = v < 0 ? -(long long)a : (long long)a;
+          }
+        }
+        __syncwarp();
+        if (tq == 0) {
+          if (shA && gq < nrows) S.escale[rA] += shA;
+          if (shB && gq + 8 < nrows) S.escale[rB] += shB;
+        }
+        __syncwarp();
+        mA = ws_scale64(mA, -shA);
+        mB = ws_scale64(mB, -shB);
+      }
       blA = mA ? 64 - __clzll((long long)mA) : 0;
       blB = mB ? 64 - __clzll((long long)mB) : 0;
     }
@@ -615,10 +646,10 @@ __global__ void __launch_bounds__(kWsThreads, kOne ? 3 : 2)
             long long nh = 0, nl = 0;
             ws_levels_of(acc, hh, nt, j, nh, nl);
             if ((nh | nl) == 0) continue;
-            // correction in the row's fixed point: (nh 2^28 + nl) 2^sh, sh = zr + fc - 63 + 62 - er
-            const int sh = zr + fc - 1 - er;
+            // correction in the row's fixed point: (nh 2^35 + nl) 2^sh, sh = zr + fc - 70 + 62 - er
+            const int sh = zr + fc - 8 - er;
             const long long ah = nh < 0 ? -nh : nh, al = nl < 0 ? -nl : nl;
-            const long long dh = (long long)ws_scale64((uint64_t)ah, sh + 28);
+            const long long dh = (long long)ws_scale64((uint64_t)ah, sh + 35);
             const long long dl = (long long)ws_scale64((uint64_t)al, sh);
             S.win[rr][(op.start + cc) & (kWsCW - 1)] -= (nh < 0 ? -dh : dh) + (nl < 0 ? -dl : dl);
           }
@@ -664,7 +695,7 @@ __global__ void __launch_bounds__(kWsThreads, kOne ? 3 : 2)
 #pragma unroll
           for (int j = 0; j < 2; ++j) ws_levels_of(acc, hh, nt, j, xh[hh][nt][j], xl[hh][nt][j]);
     }
-    // ---- X = S 2^E, E = erow + fv_m - 63 (masked); its digits as A fragments ----
+    // ---- X = S 2^E, E = erow + fv_m - 70 (masked); its digits as A fragments ----
     __int128 xs[2][2][2];
     int xe[2][2][2];
 #pragma unroll
@@ -679,7 +710,7 @@ __global__ void __launch_bounds__(kWsThreads, kOne ? 3 : 2)
           const int fvm = S.op.fv[m];
           const bool on = m >= a && m <= b && m < k && er != kWsNoScale && fvm != kWsNoScale;
           xs[hh][nt][j] = on ? ws_join(xh[hh][nt][j], xl[hh][nt][j]) : (__int128)0;
-          xe[hh][nt][j] = on ? er + fvm - 63 : 0;
+          xe[hh][nt][j] = on ? er + fvm - 70 : 0;
         }
     }
     int zrow[2];
@@ -702,7 +733,7 @@ __global__ void __launch_bounds__(kWsThreads, kOne ? 3 : 2)
             ws_levels_of(acc, hh, nt, j, yh, yl);
             const bool on = m >= a && m <= b && m < k && xr != kWsNoScale && ftm != kWsNoScale;
             xs[hh][nt][j] = on ? ws_join(yh, yl) : (__int128)0;
-            xe[hh][nt][j] = on ? xr + ftm - 63 : 0;
+            xe[hh][nt][j] = on ? xr + ftm - 70 : 0;
           }
       }
       ws_to_afrag(xs, xe, zrow, zf);
