@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--check", action="store_true", help="also compute the backward error of the last step")
     ap.add_argument("--phases", action="store_true", help="one extra serialised step for the per-phase times")
+    ap.add_argument("--save-stage1", default="", help="after the run, save this pencil's stage-1 output here")
+    ap.add_argument("--stage2-from", default="", help="time stage 2 alone on a saved stage-1 output")
     return ap.parse_args()
 
 
@@ -419,10 +421,22 @@ def main():
 
     n, r, p, nq = args.n, args.r, args.p, args.nq
     flags = ph.PARAHT_FLAG_SPLIT if args.precision == "split" else 0
-    A0, B0 = pencil(n, args.dist, seed=replica_seed(1302, rank))
+    stage2_only = bool(args.stage2_from)
+    if stage2_only:  # a saved stage-1 output (paraht_gb300.pencilio): time stage 2 alone
+        args.e2e_steps, args.check = 0, False
+        from paraht_gb300 import pencilio
+
+        head, mats = pencilio.load_pencil(args.stage2_from)
+        n, r = int(head["n"]), int(head.get("r", r))
+        A0, B0 = mats["A"], mats["B"]
+        Q0, Z0 = mats.get("Q"), mats.get("Z")
+    else:
+        A0, B0 = pencil(n, args.dist, seed=replica_seed(1302, rank))
+        Q0 = Z0 = None
     # pristine inputs on the device (column-major: a row-major tensor of the transpose)
     dev0 = [torch.from_numpy(np.ascontiguousarray(X.T)).cuda() for X in (A0, B0)]
     eye = torch.eye(n, dtype=torch.float64, device="cuda")
+    qz0 = [torch.from_numpy(np.ascontiguousarray(X.T)).cuda() if X is not None else eye for X in (Q0, Z0)]
     work = [torch.empty_like(eye) for _ in range(4)]
     ctx = ph.Context(local)
     stream = torch.cuda.Stream()
@@ -432,13 +446,16 @@ def main():
         with torch.cuda.stream(stream):
             work[0].copy_(dev0[0])
             work[1].copy_(dev0[1])
-            work[2].copy_(eye)
-            work[3].copy_(eye)
+            work[2].copy_(qz0[0])
+            work[3].copy_(qz0[1])
         stream.synchronize()
 
     def step(f=flags):
-        ctx.reduce_d(n, work[0].data_ptr(), n, work[1].data_ptr(), n, work[2].data_ptr(), n, work[3].data_ptr(), n,
-                     r, p, nq, f)
+        ptrs = (n, work[0].data_ptr(), n, work[1].data_ptr(), n, work[2].data_ptr(), n, work[3].data_ptr(), n)
+        if stage2_only:
+            ctx.rht2ht_d(*ptrs, r, nq, f)
+        else:
+            ctx.reduce_d(*ptrs, r, p, nq, f)
 
     # host-pointer entry point (the reference-facing call): pinned host buffers, copies inside
     hostA = torch.from_numpy(np.asfortranarray(A0).T.copy()).pin_memory()
@@ -459,7 +476,7 @@ def main():
 
     # warm-up: the last one goes through the host entry point (sizes its staging buffers)
     for i in range(args.warmup):
-        if i == args.warmup - 1:
+        if i == args.warmup - 1 and args.e2e_steps > 0:
             host_step()
         else:
             restore()
@@ -534,8 +551,19 @@ def main():
                     "traffic": None, "kernel": "k_apply_left/k_apply_right (FP64 compact-WY op lists)",
                     "peak_source": "FP64 FMA throughput measured on this pool's GB300 (fp64 probe)"}
 
+    if args.save_stage1 and rank == 0 and not stage2_only:
+        from paraht_gb300 import pencilio
+
+        restore()
+        ctx.ab2rht_d(n, work[0].data_ptr(), n, work[1].data_ptr(), n, work[2].data_ptr(), n, work[3].data_ptr(), n,
+                     r, p, flags & ph.PARAHT_FLAG_SPLIT)
+        torch.cuda.synchronize()
+        H1, T1, Q1, Z1 = (np.asfortranarray(w.cpu().numpy().T) for w in work)
+        pencilio.save_pencil(args.save_stage1, H1, T1, Q1, Z1, stage=1, r=r, p=p, dist=args.dist,
+                             precision=args.precision)
+
     cpu = cpu_dgghd3 = None
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and not args.no_cpu_baseline and not stage2_only:
         ns = args.cpu_sample_n
         ts = cpu_oracle_seconds(ns, r, p, nq, args.dist)
         cpu = {"value": ts * (n / ns) ** 3, "unit": "s", "cores": int(os.environ.get("OMP_NUM_THREADS",
@@ -551,7 +579,9 @@ def main():
             "metric": METRIC, "value": value, "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"HT reduction of one pencil n={n} (A N(0,1), B triangular Gaussian R), "
+            "config": {"workload": (f"stage 2 alone on the saved stage-1 output {args.stage2_from}, n={n}, "
+                                    if stage2_only else "") +
+                                   f"HT reduction of one pencil n={n} (A N(0,1), B triangular Gaussian R), "
                                    f"r={r} p={p} nq={nq}, {args.precision}",
                        "n": n, "r": r, "p": p, "nq": nq, "precision": args.precision, "dist": args.dist,
                        "parallelism": "replicas" if world > 1 else "single",
