@@ -1,7 +1,7 @@
 #!/usr/bin/env python3
 """Headline benchmark: seconds for the two-stage HT reduction of one n=16000 pencil on one GB300.
 
-Metric (BASELINE): "HT-reduction sec at n=16000: split-prec vs FP64 GPU at bwd err<=1e-13".
+Metric: "HT-reduction sec at n=16000: split-prec vs FP64 GPU at bwd err<=1e-13".
 A step is one full reduction (stage 1 + stage 2, Q and Z accumulated) of the synthetic pencil
 "std" (A ~ N(0,1), B the R factor of a Gaussian matrix, seed 1302) with the reference's
 parameter surface (r, p, nq).  Arrays are column-major FP64 resident in HBM; the pristine input
@@ -190,7 +190,7 @@ def run_reference(args, rank: int):
 
 
 BATCHES = {
-    # BASELINE configs: 4096 FP64 pencils n ~ U{32..512}; 256 pencils n log-uniform in [256, 4096],
+    # the batch workloads: 4096 FP64 pencils n ~ U{32..512}; 256 pencils n log-uniform in [256, 4096],
     # 70% Std / 30% graded-singular B, split-precision updates
     "batch4096": dict(count=4096, lo=32, hi=512, law="uniform", graded=0.0, split=False, loop=256,
                       metric="batched HT reduction: pencils/s, 4096 pencils n~U{32..512}, FP64"),

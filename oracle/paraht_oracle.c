@@ -845,8 +845,8 @@ int oracle_dgghd3(int n, double* A, int lda, double* B, int ldb, double* Q, int 
   return info;
 }
 
-/* dgghd3 with the caller's compq/compz and ilo/ihi (LAPACK's own interface), the checker of the
- * library's DGGHD3-compatible entry. */
+/* dgghd3 with the caller's compq/compz and ilo/ihi (LAPACK's own interface), the reference result
+ * for the library's DGGHD3-compatible entry in the tests. */
 int oracle_dgghd3_range(char compq, char compz, int n, int ilo, int ihi, double* A, int lda, double* B, int ldb,
                         double* Q, int ldq, double* Z, int ldz) {
   if (init_lapack()) return -100;
