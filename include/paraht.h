@@ -150,6 +150,13 @@ int paraht_gghd3_d(paraht_ctx ctx, char compq, char compz, int n, int ilo, int i
 int paraht_gghd3(char compq, char compz, int n, int ilo, int ihi, double* A, int lda, double* B, int ldb, double* Q,
                  int ldq, double* Z, int ldz, int r, int p, int nq, int flags);
 
+/* ---- failure-path self-test (no counterpart in the reference) ----
+ * Runs the pipelined chase's bounded device-side wait on a progress word that nothing sets, with
+ * a limit of spin_limit polls (1 .. 2^20, about 1 us each).  Returns the status the kernel
+ * reported: PARAHT_ERR_TIMEOUT when the wait gave up as designed (the context stays usable),
+ * 0 if it did not, PARAHT_ERR_CUDA on a launch failure, -2 for an invalid spin_limit. */
+int paraht_selftest_wait_timeout(paraht_ctx ctx, long long spin_limit);
+
 /* ---- misc ---- */
 const char* paraht_strerror(int status);
 int paraht_version(void);

@@ -144,6 +144,11 @@ class Context:
                                             IA(*ldqs), PA(*Zs), IA(*ldzs), IA(*rs), IA(*ps), IA(*nqs), int(flags)),
               "reduce_batched_d")
 
+    def selftest_wait_timeout(self, spin_limit: int = 1000) -> int:
+        """Runs the chase's bounded wait on a flag nothing sets; returns the reported status
+        (PARAHT_ERR_TIMEOUT, -1003, when the failure path works)."""
+        return int(lib().paraht_selftest_wait_timeout(self._h, int(spin_limit)))
+
     def phase_times(self) -> dict:
         buf = (C.c_double * 8)()
         check(lib().paraht_ctx_phase_times(self._h, buf, 8), "phase_times")

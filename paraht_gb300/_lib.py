@@ -54,6 +54,7 @@ SIGNATURES = {
                                 C.POINTER(_i), C.POINTER(_i), C.POINTER(_i), _i],
     "paraht_gghd3": [C.c_char, C.c_char, _i, _i, _i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i, _i, _i],
     "paraht_gghd3_d": [C.c_void_p, C.c_char, C.c_char, _i, _i, _i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i, _i, _i],
+    "paraht_selftest_wait_timeout": [C.c_void_p, C.c_longlong],
     "paraht_strerror": [_i],
     "paraht_version": [],
 }

@@ -13,6 +13,7 @@
 #include "launch_count.h"
 #include "paraht_impl.h"
 #include "paraht_internal.cuh"
+#include "s2_common.cuh"
 #include "split_apply.cuh"
 
 namespace pht {
@@ -681,6 +682,18 @@ extern "C" int paraht_reduce_batched_d(paraht_ctx c, int count, const int* n, do
   }
   if (!rc) rc = finish(x);
   x.launches = launches;
+  cudaSetDevice(prev);
+  return rc;
+}
+
+extern "C" int paraht_selftest_wait_timeout(paraht_ctx c, long long spin_limit) {
+  if (!ctx_ok(c)) return PARAHT_ERR_BAD_CTX;
+  if (spin_limit < 1 || spin_limit > (1ll << 20)) return -2;
+  Ctx& x = c->c;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(x.device);
+  const int rc = pht::s2_wait_selftest(x.stream, x.dstatus, spin_limit);
   cudaSetDevice(prev);
   return rc;
 }

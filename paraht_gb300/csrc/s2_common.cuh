@@ -30,6 +30,10 @@ struct ChaseSync {
 // Launches the band-only bulge chase of one sweep group (src/rht2ht.f90:1450-1596).
 // sequential != 0 runs every sweep in one CTA, one after the other (the reference's order);
 // otherwise one CTA per sweep, pipelined (sweep ic runs two steps behind sweep ic-1).
+// Self-test of the chase's bounded wait (see stage2_chase.cu): returns the status the wait
+// reported (PARAHT_ERR_TIMEOUT expected), words: 4 ints of device memory.
+int s2_wait_selftest(cudaStream_t st, int* words, long long spin_limit);
+
 void s2_launch_chase(cudaStream_t st, double* A, int lda, double* B, int ldb, int n, int J, int r, int nq,
                      const S2Store& S, const ChaseSync& sync, int sequential, long long spin_limit);
 
