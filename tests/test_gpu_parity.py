@@ -27,6 +27,8 @@ STAGE_CASES = [
     (257, 16, 8, 8),
     (300, 16, 4, 16),
     (333, 32, 4, 8),
+    (200, 32, 8, 8),    # L = 256: the general stage-1 generation kernels (beyond the fast ones' L <= 128)
+    (300, 64, 4, 16),   # r = 64: the widest band, L = 256
 ]
 
 
