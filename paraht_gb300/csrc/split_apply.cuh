@@ -1,7 +1,7 @@
 // split_apply.cuh -- FP64 or split-precision application of a compact-WY op list, chosen per
 // launch site.
 //
-// The FP64 kernels are in wy_apply.cuh, the split-precision (emulated FP64 on the BF16 tensor
+// The FP64 kernels are in wy_apply.cuh, the split-precision (emulated FP64 on the FP16 tensor
 // cores) kernel in wy_stream.cuh.  A left op C <- C - V T^T V^T C on column-major C is the right
 // op C^T <- C^T - C^T V T V^T on the transpose, so the split kernel sees left ops through the
 // strides (rs, cs) = (ldx, 1) and right ops through (1, ldx).
