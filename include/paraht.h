@@ -17,7 +17,7 @@
  * PARAHT_ERR_* codes below.  The reference has no error reporting (LAPACK INFO is ignored,
  * src/ab2rht.f90:105, :291); nothing here aborts the process.
  *
- * Valid parameters (checked): n >= 1; 1 <= r <= 64; p >= 2; 1 <= nq <= r.  Stage 2 must be
+ * Valid parameters (checked): n >= 0 (0: nothing to do); 1 <= r <= 64; p >= 2; 1 <= nq <= r.  Stage 2 must be
  * given the same r that stage 1 used (src/profilereduction.f90:136, :144).  nq > r lies
  * outside the domain where the reference's staircase bookkeeping (src/rht2ht.f90:1649-1675,
  * :1823-1829) stays consistent: its results lose accuracy for some n, so it is rejected.
@@ -127,7 +127,8 @@ int paraht_rht2ht_d_noalloc(paraht_ctx ctx, int n, double* A, int lda, double* B
  * pencil per run).  Pencils with p*r <= 64 and n <= PARAHT_BATCH_MAX_N are reduced by one
  * persistent launch, one CTA per pencil at a time, largest first; their results are bitwise
  * those of paraht_reduce_d in FP64 (also when PARAHT_FLAG_SPLIT is set).  The other pencils go
- * through paraht_reduce_d one after the other, overlapping the persistent launch.
+ * through the single-pencil path, largest first, up to eight at a time on internal worker
+ * contexts (own streams and workspace), overlapping the persistent launch.
  * PARAHT_FLAG_BATCH_LOOP sends every pencil through paraht_reduce_d (the looped baseline).
  * Pointers of different pencils must not overlap. ---- */
 #define PARAHT_BATCH_MAX_N 1024
