@@ -2,17 +2,20 @@
 // (A r-Hessenberg, B upper triangular), accumulating Q <- Q*Q1 and Z <- Z*Z1.
 //
 // Follows src/ab2rht.f90:8-495 (ab2rht_simple).  Per panel jb (ab2rht.f90:71):
-//   1. k_s1_left_gen      QR of the overlapping p*nb x nb blocks of the panel, bottom to top
-//                         (ab2rht.f90:85-123): reflectors VL, triangular factors TL, R into A.
+//   1. left generation: QR of the overlapping p*nb x nb blocks of the panel, bottom to top
+//      (ab2rht.f90:85-123): reflectors VL, triangular factors TL, R into A (k_s1_lgen,
+//      stage1_gen.cu; the general k_s1_left_gen below when the panel exceeds shared memory).
 //   2. left ops on B, A and right ops on Q with (VL, TL) (ab2rht.f90:135-250), all blocks in
-//      bottom-to-top order, as ordered compact-WY op lists (wy_apply.cuh).
-//   3. per block, bottom to top: k_s1_right_gen computes the RQ of the diagonal L x L block of B,
-//      the first nb rows of its orthogonal factor and their LQ (the "RQ->LQ trick",
-//      ab2rht.f90:282-312) giving nb right reflectors (VR, TR); they are applied at once to every
-//      row of B above the block's last row (ab2rht.f90:317-367) and the first nb columns of the
-//      block are zeroed below the diagonal (ab2rht.f90:329-333).
+//      bottom-to-top order, as ordered compact-WY op lists (FP64: wy_apply.cuh; split
+//      precision: wy_stream.cuh).
+//   3. per block, bottom to top: the right generation computes the RQ of the diagonal L x L
+//      block of B, the first nb rows of its orthogonal factor and their LQ (the "RQ->LQ trick",
+//      ab2rht.f90:282-312) giving nb right reflectors (VR, TR) (k_s1_rgen; k_s1_right_gen below
+//      for L > 128); they are applied to the B rows the next block needs on the critical stream
+//      and to the remaining B rows on a side stream (ab2rht.f90:317-367), and the first nb
+//      columns of the block are zeroed below the diagonal (ab2rht.f90:329-333).
 //   4. right ops on A and Z with (VR, TR), all blocks in order (ab2rht.f90:387-467).
-// The arithmetic is FP64 throughout.
+// Generation is FP64; the updates are FP64 or split precision (PARAHT_FLAG_SPLIT).
 #include <algorithm>
 
 #include "paraht_internal.cuh"

@@ -6,9 +6,11 @@
 //   1. s2_launch_chase (stage2_chase.cu): the band-only bulge chase of the group's nq columns
 //      (rht2ht.f90:1433-1596), pipelined across CTAs, producing nq left reflectors U(:,ic,ib) and
 //      nq right reflectors V(:,ic,ib) per block ib.
-//   2. k_s2_form_t: TU, TV for every block (dlarft 'F','C', rht2ht.f90:1599-1610).
+//   2. k_s2_form_t: TV for every block (dlarft 'F','C', rht2ht.f90:1599-1610; TU is built by the
+//      chase itself as the sweeps generate its columns).
 //   3. lookahead updates of B and A (rht2ht.f90:1630-1772) and the delayed bulk updates of B, A,
-//      Q and Z (rht2ht.f90:1803-2024), each an ordered compact-WY op list (wy_apply.cuh) whose
+//      Q and Z (rht2ht.f90:1803-2024), each an ordered compact-WY op list (GeoS2 in
+//      stage2_geom.cuh; FP64 kernels in wy_apply.cuh, split precision in wy_stream.cuh) whose
 //      row/column ranges are the reference's staircase (istart/istart2/istop/istop2).
 // As in the reference's task graph, the generation of group k+1 overlaps the bulk updates of
 // group k (side stream, double-buffered reflectors, rht2ht.f90:1786-1797), and the lookahead of
