@@ -1,0 +1,33 @@
+"""bench.py's reference arm runs on the host alone: one JSON line with the contract's keys
+(the CPU restatement of the reference's OpenMP algorithm, timed on a small sample)."""
+import json
+import os
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _run(*args):
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), *args], capture_output=True, text=True,
+                         timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    return json.loads(lines[0])
+
+
+def test_reference_arm_pencil_line():
+    d = _run("--impl", "reference", "--n", "2000", "--cpu-sample-n", "150", "--steps", "1", "--warmup", "1")
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+              "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert k in d, k
+    assert d["impl"] == "reference" and d["unit"] == "s" and d["higher_is_better"] is False
+    assert d["value"] > 0 and d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["value"] == d["value"]
+
+
+def test_reference_arm_batch_line():
+    d = _run("--impl", "reference", "--workload", "batch4096", "--steps", "1", "--warmup", "0")
+    assert d["impl"] == "reference" and d["unit"] == "pencils/s" and d["higher_is_better"] is True
+    assert d["value"] > 0 and "n log-U" not in d["config"]["workload"]
