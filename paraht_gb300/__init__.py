@@ -27,7 +27,7 @@ from ._lib import (PARAHT_BATCH_MAX_N, PARAHT_FLAG_BATCH_LOOP, PARAHT_FLAG_CHECK
                    ParahtError, check, lib)
 
 __all__ = [
-    "ab2rht_simple", "rht2ht_householder", "reduce", "gghd3", "Context", "ParahtError",
+    "ab2rht_simple", "rht2ht_householder", "reduce", "ht", "gghd3", "Context", "ParahtError",
     "PARAHT_FLAG_TIME_COMPONENTS", "PARAHT_FLAG_CHECK_FINITE", "PARAHT_FLAG_SPLIT", "PARAHT_FLAG_NO_ZERO_FILL",
     "PARAHT_FLAG_SEQUENTIAL", "PARAHT_FLAG_KERNEL_TIMES", "PARAHT_FLAG_BATCH_LOOP", "PARAHT_BATCH_MAX_N",
 ]
@@ -63,6 +63,29 @@ def reduce(A, B, Q, Z, r, p, nq, flags=0):
     n = A.shape[0]
     check(lib().paraht_reduce(int(n), _host_ptr(A), A.shape[0], _host_ptr(B), B.shape[0], _host_ptr(Q), Q.shape[0],
                               _host_ptr(Z), Z.shape[0], int(r), int(p), int(nq), int(flags)), "reduce")
+
+
+def ht(A, B, precision="split", params=None):
+    """Hessenberg-triangular form of the pencil (A, B), B upper triangular, as new arrays:
+    returns (H, T, Q, Z) with H = Q^T A Z upper Hessenberg and T = Q^T B Z upper triangular.
+    `precision` "split" (split-precision bulk updates) or "fp64"; `params` (r, p, nq) or None for
+    the autotuner's choice for this size (paraht_gb300.tune).  Inputs are not modified."""
+    from . import tune
+
+    if precision not in ("split", "fp64"):
+        raise ValueError("precision must be 'split' or 'fp64'")
+    H = np.array(A, dtype=np.float64, order="F", copy=True)
+    T = np.array(B, dtype=np.float64, order="F", copy=True)
+    n = H.shape[0]
+    if H.shape != (n, n) or T.shape != (n, n):
+        raise ValueError("A and B must be square and of the same size")
+    Q = np.asfortranarray(np.eye(n))
+    Z = np.asfortranarray(np.eye(n))
+    if n == 0:
+        return H, T, Q, Z
+    r, p, nq = params if params is not None else tune.pick(n, precision)
+    reduce(H, T, Q, Z, r, p, nq, PARAHT_FLAG_SPLIT if precision == "split" else 0)
+    return H, T, Q, Z
 
 
 def gghd3(compq, compz, ilo, ihi, A, B, Q, Z, r=16, p=4, nq=16, flags=0):

@@ -75,3 +75,14 @@ def test_gghd3_argument_errors():
     with pytest.raises(ph.ParahtError) as e:
         ph.gghd3("I", "I", 1, n, A, B, Q, Z, 4, 2, 8)
     assert e.value.status == -16
+
+
+def test_ht_convenience_returns_new_arrays(oracle):
+    n = 120
+    A0, B0 = pencil(n, "std", seed=21)
+    for precision in ("split", "fp64"):
+        H, T, Q, Z = ph.ht(A0, B0, precision)
+        tol = 10 * n * EPS
+        assert bwd(Q, A0, Z, H) <= tol and bwd(Q, B0, Z, T) <= tol
+        assert np.all(np.tril(H, -2) == 0.0) and np.all(np.tril(T, -1) == 0.0)
+    assert np.array_equal(A0, pencil(n, "std", seed=21)[0])  # inputs untouched
