@@ -1,20 +1,36 @@
 #!/usr/bin/env python3
-"""Headline benchmark: seconds for the two-stage HT reduction of one n=16000 pencil on one GB300.
+"""Headline benchmark: seconds for the two-stage HT reduction of one n=16000 pencil on one GB300,
+split-precision bulk updates against the all-FP64 GPU path.
 
 Metric: "HT-reduction sec at n=16000: split-prec vs FP64 GPU at bwd err<=1e-13".
 A step is one full reduction (stage 1 + stage 2, Q and Z accumulated) of the synthetic pencil
 "std" (A ~ N(0,1), B the R factor of a Gaussian matrix, seed 1302) with the reference's
-parameter surface (r, p, nq).  Arrays are column-major FP64 resident in HBM; the pristine input
-is restored (device-to-device copy) before every step, outside the timed region.  The inputs
-(4 x n^2 x 8 B = 8.2 GB at n=16000) are far larger than L2, so no extra L2 flush is needed.
+parameter surface (r, p, nq), as src/profilereduction.f90:134-148 times it: one call of each
+stage on device-resident arrays, then the backward-error report (:165-184).  Arrays are
+column-major FP64 resident in HBM; the pristine input is restored (device-to-device copy) before
+every step, outside the timed region.  The inputs (4 x n^2 x 8 B = 8.2 GB at n=16000) are far
+larger than L2, so no extra L2 flush is needed.
 
-* ``value``: mean device time per step (CUDA events on the library's stream, max over ranks).
-* ``e2e``:   the same reduction through the public host entry point paraht_reduce_host with
-             pinned host buffers, host<->device copies inside the timed region.
+One reduction at n=16000 takes minutes, so the run is bounded by a wall budget (--budget-s,
+measured from process start): the warm-up runs W-1 reductions at n=2000 and one full-size
+reduction; then one FP64 reduction at the FP64 path's own tuned parameters; then timed
+split-precision reductions until the budget left covers only the end-to-end step, the checks
+and the CPU baselines.  ``steps`` is the number of split reductions actually timed,
+``steps_requested`` the --steps asked for.
+
+* ``value``: mean device time per split step (CUDA events on the library's stream, max over ranks).
+* ``fp64``: the all-FP64 path's device time for one reduction at its tuned (r, p, nq), its
+  backward errors, and ``split_vs_fp64`` = fp64 seconds / split seconds.
+* ``check``: backward errors ||Q^T A0 Z - H||/||A0||, ||Q^T B0 Z - T||/||B0|| and orthogonality
+  ||Q^T Q - I||_F, ||Z^T Z - I||_F of the last split step (FP64 GEMMs on the device).
+* ``e2e``: one split reduction through the public host entry point paraht_reduce_host with
+  pinned host buffers, host<->device copies inside the timed region.
+* ``roofline``: the dominant kernel (the split-precision compact-WY op-list kernel of stage 2),
+  every launch timed with CUDA events on its stream during the timed steps.
 * ``cpu_baseline``: the CPU oracle (a restatement of the reference's OpenMP algorithm) on a
-             bounded sample, scaled by (n / n_sample)^3 to the metric's unit.
+  bounded sample, scaled by (n / n_sample)^3 to the metric's unit.
 * ``--impl reference``: times that CPU implementation on the host cores (the reference itself
-             is Fortran and cannot be compiled on this image).
+  is Fortran and cannot be compiled on this image).
 
 Multi-GPU: the single-pencil path does not shard (replicas only): with N ranks every rank
 reduces its own pencil; value = max-over-ranks step time / N (job seconds per reduction).
@@ -30,6 +46,7 @@ import sys
 import threading
 import time
 
+T_PROC0 = time.perf_counter()
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -37,9 +54,29 @@ import numpy as np  # noqa: E402
 
 METRIC = "HT-reduction sec at n=16000: split-prec vs FP64 GPU at bwd err<=1e-13"
 EPS = float(np.finfo(np.float64).eps)
+# FP64 roof when it cannot be measured in the run: 2 FMA/clk/SM x 152 SMs x 2.07 GHz on GB300
+FP64_PEAK_TFLOPS = 1.26
 
 
-def parse():
+def measure_fp64_peak(torch, n: int = 8192, reps: int = 3):
+    """The FP64 roof used for the FP64 kernels' roofline fraction: cuBLAS DGEMM (torch.matmul on
+    float64, 2 n^3 flops) on this GPU, best of `reps` after one warm-up, in TFLOP/s."""
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    best = float("inf")
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    del a, b
+    return 2.0 * n ** 3 / best / 1e12
+
+
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=1)
@@ -54,16 +91,27 @@ def parse():
     ap.add_argument("--r", type=int, default=16)
     ap.add_argument("--p", type=int, default=4)
     ap.add_argument("--nq", type=int, default=16)
+    ap.add_argument("--fp64-params", default="32,4,16",
+                    help="r,p,nq of the FP64 comparison step (the FP64 path's tuned parameters at n >= 4000)")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison step")
     ap.add_argument("--dist", default="std")
     ap.add_argument("--precision", choices=("fp64", "split"), default="split")
     ap.add_argument("--e2e-steps", type=int, default=1)
-    ap.add_argument("--cpu-sample-n", type=int, default=2500)
+    ap.add_argument("--cpu-sample-n", type=int, default=4000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--check", action="store_true", help="also compute the backward error of the last step")
+    ap.add_argument("--no-check", action="store_true", help="skip the backward-error / orthogonality check")
+    ap.add_argument("--check", action="store_true", help=argparse.SUPPRESS)  # the check is on by default
+    ap.add_argument("--budget-s", type=float, default=1500.0,
+                    help="wall-clock budget of the whole run in seconds, from process start")
+    ap.add_argument("--warmup-n", type=int, default=2000, help="size of the reduced-size warm-up steps")
     ap.add_argument("--phases", action="store_true", help="one extra serialised step for the per-phase times")
     ap.add_argument("--save-stage1", default="", help="after the run, save this pencil's stage-1 output here")
     ap.add_argument("--stage2-from", default="", help="time stage 2 alone on a saved stage-1 output")
-    return ap.parse_args()
+    return ap.parse_args(argv)
+
+
+def elapsed() -> float:
+    return time.perf_counter() - T_PROC0
 
 
 class ClockSampler:
@@ -124,6 +172,19 @@ def job_time(t_local: float, device) -> float:
     return float(tt.item())
 
 
+def all_agree(flag: bool, device) -> bool:
+    """True only if every rank passes True (replicas decide together whether to time another
+    step, so that all of them reach the same barriers)."""
+    import torch
+    import torch.distributed as td
+
+    if not (td.is_available() and td.is_initialized()) or td.get_world_size() == 1:
+        return flag
+    tt = torch.tensor([1 if flag else 0], dtype=torch.int32, device=device)
+    td.all_reduce(tt, op=td.ReduceOp.MIN)
+    return bool(int(tt.item()))
+
+
 def replica_seed(base: int, rank: int) -> int:
     """Seed of rank `rank`'s own input (replicas reduce different pencils of one distribution)."""
     return base + rank
@@ -132,6 +193,17 @@ def replica_seed(base: int, rank: int) -> int:
 def flops_nominal(n: int) -> float:
     # fixed nominal count used for "effective GFLOP/s" (stage 1 at p=8 plus stage 2): 18.67 n^3
     return 18.67 * float(n) ** 3
+
+
+def budget_plan(budget_s: float, now_s: float, t_step_s: float, done: int, requested: int, reserve_s: float) -> bool:
+    """Whether to time another step: always the first one, then while fewer than `requested`
+    are done and another step of t_step_s plus the work still to come (reserve_s) fits in the
+    wall budget."""
+    if done >= requested:
+        return False
+    if done == 0:
+        return True
+    return now_s + t_step_s + reserve_s <= budget_s
 
 
 def cpu_oracle_seconds(n_sample: int, r: int, p: int, nq: int, dist: str):
@@ -163,29 +235,40 @@ def cpu_dgghd3_seconds(n_sample: int, dist: str):
     return dt
 
 
+def reference_line(args, ts, ns, cores):
+    """The reference arm's JSON line: the CPU oracle's mean time per sample reduction at n=ns,
+    extrapolated by (n/ns)^3 to the workload size."""
+    scale = (args.n / ns) ** 3
+    v = statistics.mean(ts) * scale
+    return {
+        "metric": METRIC, "value": v, "unit": "s", "impl": "reference", "n_gpus": args.gpus, "steps": len(ts),
+        "steps_requested": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(ts) * 1e3,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"HT reduction n={args.n} r={args.r} p={args.p} nq={args.nq} dist={args.dist}",
+                   "n": args.n, "r": args.r, "p": args.p, "nq": args.nq},
+        "sample_n": ns, "extrapolated": True, "extrapolation": f"(n/{ns})^3 = {scale:.2f}",
+        "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port",
+                         "sample": f"oracle (C/OpenMP restatement of ab2rht_simple+rht2ht_householder, single-threaded "
+                                   f"BLAS inside tasks) at n={ns}, mean of {len(ts)} runs, scaled by (n/{ns})^3; "
+                                   f"ms_per_step is the n={ns} sample's time"},
+        "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
 def run_reference(args, rank: int):
-    """--impl reference: the CPU implementation of the path on the host cores."""
+    """--impl reference: the CPU implementation of the path on the host cores, sample reductions
+    at n = --cpu-sample-n timed until --steps are done or the wall budget runs out."""
     if rank != 0:
         return 0
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    ns = args.cpu_sample_n
+    ns = min(args.cpu_sample_n, args.n)
     for _ in range(args.warmup):
         cpu_oracle_seconds(max(200, ns // 4), args.r, args.p, args.nq, args.dist)
-    ts = [cpu_oracle_seconds(ns, args.r, args.p, args.nq, args.dist) for _ in range(max(1, args.steps))]
-    scale = (args.n / ns) ** 3
-    v = statistics.mean(ts) * scale
-    line = {
-        "metric": METRIC, "value": v, "unit": "s", "impl": "reference", "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": statistics.mean(ts) * 1e3, "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"HT reduction n={args.n} r={args.r} p={args.p} nq={args.nq} dist={args.dist}",
-                   "n": args.n, "r": args.r, "p": args.p, "nq": args.nq},
-        "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port",
-                         "sample": f"oracle (C/OpenMP restatement of ab2rht_simple+rht2ht_householder, single-threaded "
-                                   f"BLAS inside tasks) at n={ns}, mean of {len(ts)} runs, scaled by (n/{ns})^3"},
-        "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }
-    print(json.dumps(line), flush=True)
+    ts = []
+    budget = min(args.budget_s, 600.0)
+    while budget_plan(budget, elapsed(), ts[-1] if ts else 0.0, len(ts), max(1, args.steps), 0.0):
+        ts.append(cpu_oracle_seconds(ns, args.r, args.p, args.nq, args.dist))
+    print(json.dumps(reference_line(args, ts, ns, cores)), flush=True)
     return 0
 
 
@@ -363,6 +446,7 @@ def run_batch(args, rank: int, world: int, local: int):
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_rate(4 if spec["split"] else 8)[1]
     if rank == 0:
+        fp64_peak = measure_fp64_peak(torch)
         achieved = flops / t_step / 1e12 * world
         print(json.dumps({
             "metric": spec["metric"], "value": value, "unit": "pencils/s", "n_gpus": world, "steps": args.steps,
@@ -376,10 +460,10 @@ def run_batch(args, rank: int, world: int, local: int):
             "looped_baseline": {"value": loop_v, "unit": "pencils/s", "sample": len(sample),
                                 "note": "paraht_reduce_d per pencil, time per pencil scaled to the batch's mean n^3",
                                 "speedup": value / world / loop_v},
-            "roofline": {"bound": "fp64", "achieved": achieved, "peak": 1.19, "unit": "TFLOP/s",
-                         "frac": achieved / 1.19, "traffic": None,
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                         "frac": achieved / fp64_peak, "traffic": None,
                          "kernel": "k_batch_reduce and the single-pencil kernels (nominal 18.67 n^3 flops per pencil)",
-                         "peak_source": "FP64 FMA throughput measured on this pool's GB300 (fp64 probe)"},
+                         "peak_source": "cuBLAS DGEMM 8192^3 measured in this run, of measured"},
             "bwd_err": {"max": errs_sorted[-1], "p99": errs_sorted[min(len(errs) - 1, int(0.99 * len(errs)))]},
             "cpu_baseline": cpu,
             "clocks": sampler.summary(),
@@ -392,16 +476,26 @@ def run_batch(args, rank: int, world: int, local: int):
     return 0
 
 
-def main():
-    args = parse()
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if args.workload != "pencil":
-        return run_batch(args, rank, world, local)
-    if args.impl == "reference":
-        return run_reference(args, rank)
 
+
+def device_check(torch, work, dev0):
+    """Backward errors ||Q^T X0 Z - X||_F / ||X0||_F (src/profilereduction.f90:165-174) and
+    orthogonality ||Q^T Q - I||_F, ||Z^T Z - I||_F of a reduced pencil, FP64 GEMMs on the device.
+    The arrays are column-major data held as row-major tensors of the transposes."""
+    H, T, Q, Z = (w.T for w in work)
+    Af, Bf = dev0[0].T, dev0[1].T
+    n = H.shape[0]
+    out = {}
+    out["bwd_err_A"] = float(torch.linalg.norm(Q.T @ Af @ Z - H) / torch.linalg.norm(Af))
+    out["bwd_err_B"] = float(torch.linalg.norm(Q.T @ Bf @ Z - T) / torch.linalg.norm(Bf))
+    eye = torch.eye(n, dtype=torch.float64, device=H.device)
+    out["orth_Q_fro"] = float(torch.linalg.norm(Q.T @ Q - eye))
+    out["orth_Z_fro"] = float(torch.linalg.norm(Z.T @ Z - eye))
+    out["below_structure_nonzeros"] = int(torch.count_nonzero(torch.tril(H, -2)) + torch.count_nonzero(torch.tril(T, -1)))
+    return out
+
+
+def run_pencil(args, rank: int, world: int, local: int):
     import torch
 
     import paraht_gb300 as ph
@@ -423,10 +517,14 @@ def main():
             td.barrier()
 
     n, r, p, nq = args.n, args.r, args.p, args.nq
-    flags = ph.PARAHT_FLAG_SPLIT if args.precision == "split" else 0
+    split = args.precision == "split"
+    flags = ph.PARAHT_FLAG_SPLIT if split else 0
+    fr, fp, fnq = (int(x) for x in args.fp64_params.split(","))
+    do_fp64 = split and not args.no_fp64
+    do_check = not args.no_check
     stage2_only = bool(args.stage2_from)
     if stage2_only:  # a saved stage-1 output (paraht_gb300.pencilio): time stage 2 alone
-        args.e2e_steps, args.check = 0, False
+        args.e2e_steps, do_check, do_fp64 = 0, False, False
         from paraht_gb300 import pencilio
 
         head, mats = pencilio.load_pencil(args.stage2_from)
@@ -445,87 +543,133 @@ def main():
     stream = torch.cuda.Stream()
     ctx.set_stream(stream.cuda_stream)
 
-    def restore():
+    def restore(w=work, src=None):
+        a, b, q, z = src if src is not None else (dev0[0], dev0[1], qz0[0], qz0[1])
         with torch.cuda.stream(stream):
-            work[0].copy_(dev0[0])
-            work[1].copy_(dev0[1])
-            work[2].copy_(qz0[0])
-            work[3].copy_(qz0[1])
+            w[0].copy_(a)
+            w[1].copy_(b)
+            w[2].copy_(q)
+            w[3].copy_(z)
         stream.synchronize()
 
-    def step(f=flags):
-        ptrs = (n, work[0].data_ptr(), n, work[1].data_ptr(), n, work[2].data_ptr(), n, work[3].data_ptr(), n)
+    def launch(w, m, prm, f):
+        rr, pp, qq = prm
+        ptrs = (m, w[0].data_ptr(), m, w[1].data_ptr(), m, w[2].data_ptr(), m, w[3].data_ptr(), m)
         if stage2_only:
-            ctx.rht2ht_d(*ptrs, r, nq, f)
+            ctx.rht2ht_d(*ptrs, rr, qq, f)
         else:
-            ctx.reduce_d(*ptrs, r, p, nq, f)
+            ctx.reduce_d(*ptrs, rr, pp, qq, f)
 
-    # host-pointer entry point (the reference-facing call): pinned host buffers, copies inside
-    hostA = torch.from_numpy(np.asfortranarray(A0).T.copy()).pin_memory()
-    hostB = torch.from_numpy(np.asfortranarray(B0).T.copy()).pin_memory()
-    hostQ = torch.empty((n, n), dtype=torch.float64).pin_memory()
-    hostZ = torch.empty((n, n), dtype=torch.float64).pin_memory()
-
-    def host_step():
-        hostA.copy_(torch.from_numpy(np.asfortranarray(A0).T))
-        hostB.copy_(torch.from_numpy(np.asfortranarray(B0).T))
-        hostQ.copy_(torch.eye(n, dtype=torch.float64))
-        hostZ.copy_(torch.eye(n, dtype=torch.float64))
-        nA, nB, nQ, nZ = (x.numpy().T for x in (hostA, hostB, hostQ, hostZ))  # Fortran-ordered views
+    def timed(prm, f):
+        """One reduction of the full pencil on `work`; device seconds (CUDA events on the stream)."""
+        restore()
         barrier()
-        t0 = time.perf_counter()
-        ctx.reduce_host(nA, nB, nQ, nZ, r, p, nq, flags)
-        return time.perf_counter() - t0
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        launch(work, n, prm, f)
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / 1e3
 
-    # warm-up: the last one goes through the host entry point (sizes its staging buffers)
-    for i in range(args.warmup):
-        if i == args.warmup - 1 and args.e2e_steps > 0:
-            host_step()
-        else:
-            restore()
-            step()
+    # ---- warm-up: W-1 reductions at a reduced size (each parameter set used later), then one at
+    # full size (module loading, workspace sizing, operand slots) ----
+    nw = min(n, args.warmup_n)
+    small0 = pencil(nw, args.dist, seed=7)
+    sdev = [torch.from_numpy(np.ascontiguousarray(X.T)).cuda() for X in small0]
+    seye = torch.eye(nw, dtype=torch.float64, device="cuda")
+    swork = [torch.empty_like(seye) for _ in range(4)]
+    warm_sets = [((r, p, nq), flags)] + ([((fr, fp, fnq), 0)] if do_fp64 else [])
+    for i in range(max(0, args.warmup - 1)):
+        prm, f = warm_sets[i % len(warm_sets)]
+        restore(swork, (sdev[0], sdev[1], seye, seye))
+        launch(swork, nw, prm, f)
+    if do_fp64 and args.warmup < 3:  # the FP64 parameter set gets at least one small warm-up
+        restore(swork, (sdev[0], sdev[1], seye, seye))
+        launch(swork, nw, (fr, fp, fnq), 0)
+    del swork, sdev, seye
+    t0w = time.perf_counter()
+    if args.warmup > 0:
+        restore()
+        launch(work, n, (r, p, nq), flags)
     torch.cuda.synchronize()
-    ms = []
-    launches = 0
+    t_warm_full = time.perf_counter() - t0w
+
+    try:
+        fp64_peak = measure_fp64_peak(torch)
+    except RuntimeError:
+        fp64_peak = FP64_PEAK_TFLOPS
+    ms, launches = [], 0
     kst = {"stage1": {"seconds": 0.0, "launches": 0, "flops": 0.0}, "stage2": {"seconds": 0.0, "launches": 0, "flops": 0.0}}
+    fp64 = None
+    check = None
+    t_check = 0.0
     sampler = ClockSampler(local)
     with sampler:
-        for _ in range(args.steps):
-            restore()
-            barrier()
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            step(flags | ph.PARAHT_FLAG_KERNEL_TIMES)
-            e1.record(stream)
-            e1.synchronize()
-            ms.append(e0.elapsed_time(e1))
+        # ---- one FP64 reduction at the FP64 path's own parameters ----
+        if do_fp64:
+            t_f = timed((fr, fp, fnq), ph.PARAHT_FLAG_KERNEL_TIMES)
+            t_f = job_time(t_f, "cuda")
+            fst = ctx.kernel_stats()["stage2"]
+            fp64 = {"seconds": t_f, "r": fr, "p": fp, "nq": fnq, "launches": ctx.launch_count(),
+                    "effective_gflops": flops_nominal(n) / t_f / 1e9,
+                    "op_list_kernel": {"kernel": "k_apply_left/k_apply_right<GeoS2> (FP64 compact-WY op lists)",
+                                       "achieved_tflops": fst["flops"] / fst["seconds"] / 1e12 if fst["seconds"] > 0 else None,
+                                       "peak_tflops": fp64_peak,
+                                       "peak_source": "cuBLAS DGEMM 8192^3 measured in this run, of measured",
+                                       "frac": (fst["flops"] / fst["seconds"] / 1e12 / fp64_peak
+                                                if fst["seconds"] > 0 else None),
+                                       "launches": fst["launches"], "seconds": fst["seconds"]}}
+            if do_check:
+                tc = time.perf_counter()
+                fp64["check"] = device_check(torch, work, dev0)
+                t_check = time.perf_counter() - tc
+        # ---- timed split (or --precision) reductions within the budget ----
+        t_est = t_warm_full
+        cpu_est = 0.0 if (args.no_cpu_baseline or rank != 0 or stage2_only) else 90.0 * (min(args.cpu_sample_n, n) / 4000.0) ** 3 + 10.0
+        e2e_est = (t_est * 1.05 + 5.0) * max(0, args.e2e_steps)
+        reserve = e2e_est + (t_check if do_check else 0.0) + cpu_est + 20.0
+        while all_agree(budget_plan(args.budget_s, elapsed(), t_est, len(ms), max(1, args.steps), reserve), "cuda"):
+            ms.append(timed((r, p, nq), flags | ph.PARAHT_FLAG_KERNEL_TIMES))
+            t_est = max(t_est, ms[-1] * 1.02)
             launches += ctx.launch_count()
             st = ctx.kernel_stats()
             for k in kst:
                 for f in kst[k]:
                     kst[k][f] += st[k][f]
             barrier()
-    t_step = statistics.mean(ms) / 1e3
-    t_step = job_time(t_step, "cuda")
+    steps_done = len(ms)
+    t_step = job_time(statistics.mean(ms), "cuda")
     value = t_step / world
 
-    # backward error of the last timed step (outside the timed region)
-    check = None
-    if args.check:
-        H, T, Q, Z = work[0].T, work[1].T, work[2].T, work[3].T
-        Af, Bf = dev0[0].T, dev0[1].T  # column-major data stored as row-major transposes
-        ea = float(torch.linalg.norm(Q.T @ Af @ Z - H) / torch.linalg.norm(Af))
-        eb = float(torch.linalg.norm(Q.T @ Bf @ Z - T) / torch.linalg.norm(Bf))
-        check = {"bwd_err_A": ea, "bwd_err_B": eb, "bound_10n_eps": 10 * n * EPS}
+    # backward errors and orthogonality of the last timed step (outside the timed region)
+    if do_check:
+        check = device_check(torch, work, dev0)
+        check["bound_split"] = 1e-13
+        check["bound_10n_eps"] = 10 * n * EPS
 
     # end to end through the host entry point, copies inside the timed region
-    e2e_v = statistics.mean([host_step() for _ in range(args.e2e_steps)]) / world if args.e2e_steps > 0 else None
+    hbuf = [torch.empty((n, n), dtype=torch.float64).pin_memory() for _ in range(4)] if args.e2e_steps > 0 else []
+
+    def host_step():
+        hbuf[0].copy_(torch.from_numpy(np.asfortranarray(A0).T))
+        hbuf[1].copy_(torch.from_numpy(np.asfortranarray(B0).T))
+        hbuf[2].copy_(torch.eye(n, dtype=torch.float64))
+        hbuf[3].copy_(torch.eye(n, dtype=torch.float64))
+        nA, nB, nQ, nZ = (x.numpy().T for x in hbuf)  # Fortran-ordered views of pinned memory
+        barrier()
+        t0 = time.perf_counter()
+        ctx.reduce_host(nA, nB, nQ, nZ, r, p, nq, flags)
+        return time.perf_counter() - t0
+
+    e2e_v = None
+    if args.e2e_steps > 0:
+        e2e_v = job_time(statistics.mean([host_step() for _ in range(args.e2e_steps)]), "cuda") / world
 
     phases = None
     if args.phases:  # time_components serialises the streams: one extra, slower step
         restore()
-        step(flags | ph.PARAHT_FLAG_TIME_COMPONENTS)
+        launch(work, n, (r, p, nq), flags | ph.PARAHT_FLAG_TIME_COMPONENTS)
         phases = {k: round(v, 4) for k, v in ctx.phase_times().items()}
 
     # roofline of the dominant kernel: the compact-WY op-list kernel of stage 2 (bulk and
@@ -533,28 +677,34 @@ def main():
     # steps; its algorithmic work is 4 len k FP64-equivalent flops per strip row per op
     peaks = {}
     try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            peaks = json.load(fh)
+    except (OSError, ValueError):
         pass
     s2 = kst["stage2"]
-    if args.precision == "split":
+    fp64eq = s2["flops"] / s2["seconds"] / 1e12 if s2["seconds"] > 0 else None
+    if split:
         # each FP64-equivalent flop is 43 FP16 digit-pair flops on the tensor cores (pairs t+u <= 8)
         measured = "bf16_tflops" in peaks
         peak = float(peaks["bf16_tflops"]) if measured else 1900.0
-        achieved = 43.0 * s2["flops"] / s2["seconds"] / 1e12 if s2["seconds"] > 0 else None
+        achieved = 43.0 * fp64eq if fp64eq else None
         roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                     "frac": achieved / peak if achieved else None, "traffic": None,
                     "kernel": "k_ws_apply<GeoS2> (split-precision compact-WY op lists, FP16 digit MMAs)",
+                    "work": "4 len k FP64-equivalent flops per strip row per op, x43 FP16 digit-pair products",
                     "peak_source": ("MEASURED_PEAKS.json bf16_tflops (FP16 and BF16 mma run at the same rate), of measured"
                                     if measured else "1.9 PFLOP/s BF16 burst, of fallback (no MEASURED_PEAKS.json)"),
-                    "fp64_equivalent_tflops": s2["flops"] / s2["seconds"] / 1e12 if s2["seconds"] > 0 else None,
-                    "launches_per_step": s2["launches"] / max(1, args.steps),
+                    "fp64_equivalent_tflops": fp64eq,
+                    "launches_per_step": s2["launches"] / max(1, steps_done),
                     "avg_launch_ms": 1e3 * s2["seconds"] / max(1, s2["launches"])}
     else:
-        fp64_peak = 1.19  # TFLOP/s, FP64 FMA throughput measured on this machine's GB300
-        roofline = {"bound": "fp64", "achieved": None, "peak": fp64_peak, "unit": "TFLOP/s", "frac": None,
-                    "traffic": None, "kernel": "k_apply_left/k_apply_right (FP64 compact-WY op lists)",
-                    "peak_source": "FP64 FMA throughput measured on this pool's GB300 (fp64 probe)"}
+        roofline = {"bound": "fp64", "achieved": fp64eq, "peak": fp64_peak, "unit": "TFLOP/s",
+                    "frac": fp64eq / fp64_peak if fp64eq else None, "traffic": None,
+                    "kernel": "k_apply_left/k_apply_right<GeoS2> (FP64 compact-WY op lists)",
+                    "work": "4 len k flops per strip row per op",
+                    "peak_source": "cuBLAS DGEMM 8192^3 measured in this run, of measured",
+                    "launches_per_step": s2["launches"] / max(1, steps_done),
+                    "avg_launch_ms": 1e3 * s2["seconds"] / max(1, s2["launches"])}
 
     if args.save_stage1 and rank == 0 and not stage2_only:
         from paraht_gb300 import pencilio
@@ -569,20 +719,25 @@ def main():
 
     cpu = cpu_dgghd3 = None
     if rank == 0 and not args.no_cpu_baseline and not stage2_only:
-        ns = args.cpu_sample_n
+        ns = min(args.cpu_sample_n, n)
         ts = cpu_oracle_seconds(ns, r, p, nq, args.dist)
-        cpu = {"value": ts * (n / ns) ** 3, "unit": "s", "cores": int(os.environ.get("OMP_NUM_THREADS",
-                                                                                        os.cpu_count() or 1)),
-               "kind": "port",
+        cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+        cpu = {"value": ts * (n / ns) ** 3, "unit": "s", "cores": cores, "kind": "port", "sample_n": ns,
+               "extrapolated": ns != n,
                "sample": f"CPU oracle (OpenMP restatement of the reference) at n={ns}: {ts:.2f} s, scaled by (n/{ns})^3"}
-        td3 = cpu_dgghd3_seconds(ns, args.dist)
-        cpu_dgghd3 = {"value": td3 * (n / ns) ** 3, "unit": "s", "cores": os.cpu_count() or 1,
-                      "sample": f"LAPACK DGGHD3 (scipy's OpenBLAS, all cores) at n={ns}: {td3:.2f} s, scaled by (n/{ns})^3"}
+        nd = ns if elapsed() + 60.0 < args.budget_s + 200.0 else min(ns, 2000)
+        td3 = cpu_dgghd3_seconds(nd, args.dist)
+        cpu_dgghd3 = {"value": td3 * (n / nd) ** 3, "unit": "s", "cores": os.cpu_count() or 1, "sample_n": nd,
+                      "extrapolated": nd != n,
+                      "sample": f"LAPACK DGGHD3 (scipy's OpenBLAS, all cores) at n={nd}: {td3:.2f} s, scaled by (n/{nd})^3"}
 
     if rank == 0:
         line = {
-            "metric": METRIC, "value": value, "unit": "s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False,
+            "metric": METRIC, "value": value, "unit": "s", "n_gpus": world, "steps": steps_done,
+            "steps_requested": args.steps, "warmup": args.warmup,
+            "warmup_detail": (f"{max(0, args.warmup - 1)} reductions at n={nw}, then 1 at n={n}"
+                              if args.warmup > 0 else "none"),
+            "ms_per_step": t_step * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": (f"stage 2 alone on the saved stage-1 output {args.stage2_from}, n={n}, "
                                     if stage2_only else "") +
@@ -590,16 +745,21 @@ def main():
                                    f"r={r} p={p} nq={nq}, {args.precision}",
                        "n": n, "r": r, "p": p, "nq": nq, "precision": args.precision, "dist": args.dist,
                        "parallelism": "replicas" if world > 1 else "single",
-                       "l2": "inputs 8.2 GB >> L2; pristine input restored between steps outside the timed region"},
+                       "l2": "inputs 8.2 GB >> L2; pristine input restored between steps outside the timed region",
+                       "budget_s": args.budget_s},
             "e2e": ({"value": e2e_v, "unit": "s", "h2d_bytes_per_step": 4 * n * n * 8, "d2h_bytes_per_step": 4 * n * n * 8}
                     if e2e_v is not None else None),
-            "gpu_launches": launches,
+            "gpu_launches": launches // max(1, steps_done),
             "effective_gflops": flops_nominal(n) / t_step / 1e9,
             "roofline": roofline,
             "cpu_baseline": cpu,
             "cpu_dgghd3": cpu_dgghd3,
             "clocks": sampler.summary(),
+            "wall_s": elapsed(),
         }
+        if fp64 is not None:
+            line["fp64"] = fp64
+            line["split_vs_fp64"] = fp64["seconds"] / t_step
         if check:
             line["check"] = check
         if phases:
@@ -611,6 +771,18 @@ def main():
         td.destroy_process_group()
     ctx.close()
     return 0
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.workload != "pencil":
+        return run_batch(args, rank, world, local)
+    if args.impl == "reference":
+        return run_reference(args, rank)
+    return run_pencil(args, rank, world, local)
 
 
 if __name__ == "__main__":

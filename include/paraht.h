@@ -54,8 +54,9 @@ extern "C" {
 #define PARAHT_FLAG_SEQUENTIAL 16     /* debug: run the stage-2 sweeps of a group one after the other in
                                          one CTA and all updates on one stream (the reference's order);
                                          results are bitwise identical to the default pipelined schedule */
-#define PARAHT_FLAG_KERNEL_TIMES 32   /* time every split-precision op-list launch with CUDA events and
-                                         count its algorithmic work (paraht_ctx_kernel_stats) */
+#define PARAHT_FLAG_KERNEL_TIMES 32   /* time every bulk compact-WY op-list launch (split-precision or FP64)
+                                         with CUDA events and count its algorithmic work
+                                         (paraht_ctx_kernel_stats) */
 
 typedef struct paraht_ctx_s* paraht_ctx;
 
@@ -75,10 +76,11 @@ int paraht_ctx_launch_count(paraht_ctx ctx, long long* count);
 /* Largest absolute entry found below the structure (r-Hessenberg / Hessenberg for A,
  * triangular for B) before it was zeroed by the last call: [0] A, [1] B. */
 int paraht_ctx_fill_residue(paraht_ctx ctx, double* residue, int nres);
-/* With PARAHT_FLAG_KERNEL_TIMES, for the split-precision compact-WY op-list kernel of the last
- * call: [0] summed launch durations (s), [1] launches, [2] algorithmic FP64-equivalent flops
- * (4 len k per strip row per op) of the stage-1 lists; [3..5] the same for the stage-2 lists.
- * No counterpart in the reference. */
+/* With PARAHT_FLAG_KERNEL_TIMES, for the bulk compact-WY op-list kernels of the last call (the
+ * split-precision kernel under PARAHT_FLAG_SPLIT, else the FP64 kernels; the FP64 path's 8-row
+ * critical-path lists are not timed): [0] summed launch durations (s), [1] launches,
+ * [2] algorithmic FP64-equivalent flops (4 len k per strip row per op) of the stage-1 lists;
+ * [3..5] the same for the stage-2 lists.  No counterpart in the reference. */
 int paraht_ctx_kernel_stats(paraht_ctx ctx, double* stats, int nstats);
 
 /* ---- host-pointer drop-ins (copy in, reduce on the GPU, copy out) ----
@@ -109,15 +111,23 @@ int paraht_reduce_d(paraht_ctx ctx, int n, double* A, int lda, double* B, int ld
                     int ldz, int r, int p, int nq, int flags);
 
 /* ---- stage 2 without any allocation.  No counterpart in the reference.
- * Same arithmetic and results as paraht_rht2ht_d (FP64 only), but the scratch (reflector
- * stores, progress words) lives in a fixed file-scope device array of
+ * For callers that must not allocate device memory during the call (an application that owns
+ * all device memory through its own pool, or code running where a cudaMalloc would synchronise
+ * the device): same arithmetic and results as paraht_rht2ht_d (FP64 only), but the scratch
+ * (reflector stores, progress words) lives in a fixed file-scope device array of
  * PARAHT_NOALLOC_SCRATCH_BYTES bytes instead of the context's workspace, so the call performs
- * no cudaMalloc/cudaFree.  Returns PARAHT_ERR_TOO_LARGE if (n, r, nq) need more scratch than
- * that (about n <= 4000 for r = nq = 16), PARAHT_ERR_NOT_SUPPORTED for PARAHT_FLAG_SPLIT or
- * PARAHT_FLAG_TIME_COMPONENTS.  The scratch is shared by all callers on a device: calls that
- * overlap in time (other threads, other contexts on the same device) race.  The first call on a
- * device resolves the array's address (cudaGetSymbolAddress) and should precede any stream
- * capture.  Everything that must start at zero is cleared on the stream by the call itself. ---- */
+ * no cudaMalloc/cudaFree and creates no events.
+ * Size limit: the scratch needed is
+ *     32 b nq (r + 2 nq + 1) + 4 (nq + 2) + 4096 bytes,  b = max(1, ceil((n-1)/r)) + 2,
+ * which must not exceed PARAHT_NOALLOC_SCRATCH_BYTES (n <= 5313 for r = nq = 16, 15841 for
+ * r = 16, nq = 8, 1217 for r = nq = 64); larger inputs return PARAHT_ERR_TOO_LARGE.
+ * Flags: only PARAHT_FLAG_CHECK_FINITE, PARAHT_FLAG_NO_ZERO_FILL and PARAHT_FLAG_SEQUENTIAL are
+ * accepted; any other bit returns PARAHT_ERR_NOT_SUPPORTED.  The scratch is shared by all
+ * callers on a device and keeps the last call's contents; the library serialises the calls that
+ * host threads of one process make, and work that overlaps a call on the GPU and uses the same
+ * array (a graph or stream replaying such a call) races with it.  Every call looks up the
+ * array's device address (cudaGetSymbolAddress) with its context's device current.  Everything
+ * that must start at zero is cleared on the stream by the call itself. ---- */
 #define PARAHT_NOALLOC_SCRATCH_BYTES (8u << 20)
 int paraht_rht2ht_d_noalloc(paraht_ctx ctx, int n, double* A, int lda, double* B, int ldb, double* Q, int ldq,
                             double* Z, int ldz, int r, int nq, int flags);

@@ -79,6 +79,11 @@ def ht(A, B, precision="split", params=None):
     n = H.shape[0]
     if H.shape != (n, n) or T.shape != (n, n):
         raise ValueError("A and B must be square and of the same size")
+    if n > 1 and np.any(np.tril(T, -1) != 0.0):
+        # the reduction assumes it, as the reference's ab2rht_simple does (src/profilereduction.f90:117-123
+        # triangularises B before the call); a general B would give a wrong (H, T, Q, Z) silently
+        raise ValueError("B must be upper triangular (triangularise it first, e.g. by a QR factorisation, "
+                         "and apply the orthogonal factor's transpose to A)")
     Q = np.asfortranarray(np.eye(n))
     Z = np.asfortranarray(np.eye(n))
     if n == 0:

@@ -437,9 +437,14 @@ extern "C" int paraht_reduce_d(paraht_ctx c, int n, double* A, int lda, double* 
 }
 
 // ---- stage 2 without allocation: the workspace is a fixed file-scope device array ----
+// For callers that cannot allocate during the call (their own memory pool owns the device, or a
+// cudaMalloc would synchronise work they keep in flight).  In host code the array's name is only
+// a host-side stand-in, so its device address is looked up on every call with the context's
+// device current (a cached address would go stale after a cudaDeviceReset or under another
+// context).  Calls that overlap on the GPU share the array and race.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[PARAHT_NOALLOC_SCRATCH_BYTES];
 static std::mutex g_noalloc_mu;
-static void* g_noalloc_addr[64];  // per device, resolved once
+static constexpr int kNoallocFlags = PARAHT_FLAG_CHECK_FINITE | PARAHT_FLAG_NO_ZERO_FILL | PARAHT_FLAG_SEQUENTIAL;
 
 extern "C" int paraht_rht2ht_d_noalloc(paraht_ctx c, int n, double* A, int lda, double* B, int ldb, double* Q,
                                        int ldq, double* Z, int ldz, int r, int nq, int flags) {
@@ -447,25 +452,22 @@ extern "C" int paraht_rht2ht_d_noalloc(paraht_ctx c, int n, double* A, int lda, 
   Ctx& x = c->c;
   int rc = check_args(2, 1, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, 2, nq);
   if (rc) return rc;
-  if (flags & (PARAHT_FLAG_SPLIT | PARAHT_FLAG_TIME_COMPONENTS)) return PARAHT_ERR_NOT_SUPPORTED;
+  // the flags that would allocate (split-precision operand slots, kernel-time counters) or
+  // create events (phase and kernel timing) are refused
+  if (flags & ~kNoallocFlags) return PARAHT_ERR_NOT_SUPPORTED;
   if (pht::s2_workspace_bytes(n, r, nq) > (size_t)PARAHT_NOALLOC_SCRATCH_BYTES) return PARAHT_ERR_TOO_LARGE;
-  if (x.device < 0 || x.device >= 64) return PARAHT_ERR_NO_DEVICE;
   int prev = 0;
   cudaGetDevice(&prev);
-  cudaSetDevice(x.device);
+  if (cudaSetDevice(x.device) != cudaSuccess) {
+    cudaGetLastError();
+    return PARAHT_ERR_CUDA;
+  }
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);  // one call at a time from this process
   void* scratch = nullptr;
-  {
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_addr[x.device]) {
-      void* a = nullptr;
-      if (cudaGetSymbolAddress(&a, g_noalloc_scratch) != cudaSuccess || !a) {
-        cudaGetLastError();
-        cudaSetDevice(prev);
-        return PARAHT_ERR_CUDA;
-      }
-      g_noalloc_addr[x.device] = a;
-    }
-    scratch = g_noalloc_addr[x.device];
+  if (cudaGetSymbolAddress(&scratch, g_noalloc_scratch) != cudaSuccess || !scratch) {
+    cudaGetLastError();
+    cudaSetDevice(prev);
+    return PARAHT_ERR_CUDA;
   }
   for (double& v : x.phase) v = 0.0;
   x.residue[0] = x.residue[1] = 0.0;

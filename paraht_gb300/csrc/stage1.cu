@@ -73,19 +73,22 @@ __device__ void form_t_backward(int k, const double* G, int kg, const double* ta
 // Left generation (ab2rht.f90:85-123): for each block bottom to top, Householder QR
 // (dgeqr2 semantics) of A(ib:ib2, jb:jb+nb-1); store VL explicitly (unit diagonal, zeros
 // above), write R (zeros below) back to A, form TL (dlarft 'F','C').
-// Shared memory: P tile (L x nb, ld L+1) + G (nb x nb) + Ts (nb x nb) + tau (nb) + reduction.
+// Shared memory: G (nb x nb) + Ts (nb x nb) + tau (nb) + reduction, then the P tile (L x nb,
+// ld L+1) when it fits; otherwise the tile lives in the global scratch `gscratch` (L2-resident,
+// same code path), which lets L = p nb reach 1024 (r = 64, p = 16).
 // ------------------------------------------------------------------------------------------
 constexpr int kGenThreads = 256;
 
 __global__ void __launch_bounds__(kGenThreads) k_s1_left_gen(double* __restrict__ A, int lda, S1Panel P,
-                                                             double* __restrict__ VL, double* __restrict__ TL) {
+                                                             double* __restrict__ VL, double* __restrict__ TL,
+                                                             double* __restrict__ gscratch) {
   extern __shared__ double sm[];
   const int L = P.L, nb = P.nb, ldp = L + 1;
-  double* Pt = sm;                    // ldp * nb
-  double* G = Pt + (size_t)ldp * nb;  // nb*nb
+  double* G = sm;                     // nb*nb
   double* Ts = G + nb * nb;           // nb*nb
   double* tau = Ts + nb * nb;         // nb
   double* red = tau + nb;             // 32
+  double* Pt = gscratch ? gscratch : red + 32;  // ldp * nb
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5, nwarp = blockDim.x >> 5;
   const int jb0 = P.jb0;
   for (int o = 0; o < P.nblocks; ++o) {
@@ -349,7 +352,8 @@ size_t s1_workspace_bytes(int n, int nb, int p) {
   return w * sizeof(double) + 4096;
 }
 
-static size_t left_gen_smem(int L, int nb) { return sizeof(double) * ((size_t)(L + 1) * nb + 2 * nb * nb + nb + 32); }
+static size_t left_gen_small(int nb) { return sizeof(double) * ((size_t)2 * nb * nb + nb + 32); }
+static size_t left_gen_tile(int L, int nb) { return sizeof(double) * (size_t)(L + 1) * nb; }
 static size_t right_gen_small(int L, int nb) {
   return sizeof(double) * ((size_t)L + nb + 2 * (size_t)nb * nb + 32 + kRgenThreads);
 }
@@ -392,7 +396,8 @@ int s1_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
   // general kernels above
   const bool fast_l = nb <= 64 && s1_lgen_smem(L, nb) <= (size_t)ctx.max_smem;
   const bool fast_r = L <= 128 && s1_rgen_smem_vr(L, nb, false) <= (size_t)ctx.max_smem;
-  const size_t lsm = left_gen_smem(L, nb);
+  const bool l_in_smem = left_gen_small(nb) + left_gen_tile(L, nb) <= (size_t)ctx.max_smem;
+  const size_t lsm = l_in_smem ? left_gen_small(nb) + left_gen_tile(L, nb) : left_gen_small(nb);
   const size_t rsm_small = right_gen_small(L, nb);
   const bool r_in_smem = rsm_small + right_gen_big(L, nb) <= (size_t)ctx.max_smem;
   const size_t rsm = r_in_smem ? rsm_small + right_gen_big(L, nb) : rsm_small;
@@ -430,7 +435,7 @@ int s1_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
       launch_s1_lgen(sA, A, lda, P, VL[s], TL[s]);
     } else {
       count_launch();
-      k_s1_left_gen<<<1, kGenThreads, lsm, sA>>>(A, lda, P, VL[s], TL[s]);
+      k_s1_left_gen<<<1, kGenThreads, lsm, sA>>>(A, lda, P, VL[s], TL[s], l_in_smem ? nullptr : gscr);
     }
     if (timer) timer->mark(sA, 2);
     if (!serial) {

@@ -20,9 +20,11 @@ constexpr int kRightCCH = 64;  // column chunk staged in shared memory
 constexpr int kMaxK = 64;      // max reflectors per op
 
 // X <- H^T X on the column strip [cbeg, cend] (at most kLeftCS columns) for every op
-// (dlarfb 'L','T','F','C'); kApplyThreads threads, shared memory kLeftSmem at smx.
+// (dlarfb 'L','T','F','C'); kApplyThreads threads, shared memory kLeftSmem at smx.  When
+// `flops` is given, the op's algorithmic work (4 len k flops per column) is added to it.
 template <class Geo>
-__device__ void apply_left_strip(double* __restrict__ X, int ldx, int cbeg, int cend, const Geo& g, double* smx) {
+__device__ void apply_left_strip(double* __restrict__ X, int ldx, int cbeg, int cend, const Geo& g, double* smx,
+                                 unsigned long long* flops = nullptr) {
   double(*Xs)[kLeftCS + 1] = reinterpret_cast<double(*)[kLeftCS + 1]>(smx);
   double(*W)[kLeftCS + 1] = reinterpret_cast<double(*)[kLeftCS + 1]>(smx + kLeftRCH * (kLeftCS + 1));
   const int t = threadIdx.x;
@@ -33,6 +35,7 @@ __device__ void apply_left_strip(double* __restrict__ X, int ldx, int cbeg, int 
     if (ca > cb || op.k <= 0 || op.len <= 0) continue;
     const int w = cb - ca + 1;
     const int k = op.k;
+    if (flops && t == 0) atomicAdd(flops, 4ull * (unsigned long long)op.len * (unsigned long long)k * (unsigned long long)w);
     // ---- pass 1: W = V^T X_sub (k x w) ----
     for (int i = t; i < kMaxK * kLeftCS; i += kApplyThreads) W[i / kLeftCS][i % kLeftCS] = 0.0;
     for (int r0 = 0; r0 < op.len; r0 += kLeftRCH) {
@@ -101,11 +104,11 @@ __device__ void apply_left_strip(double* __restrict__ X, int ldx, int cbeg, int 
 
 template <class Geo>
 __global__ void __launch_bounds__(kApplyThreads) k_apply_left(double* __restrict__ X, int ldx, int col0, int col1,
-                                                               Geo g) {
+                                                               Geo g, unsigned long long* flops) {
   extern __shared__ double smx[];
   const int cbeg = col0 + blockIdx.x * kLeftCS;
   if (cbeg > col1) return;
-  apply_left_strip(X, ldx, cbeg, min(col1, cbeg + kLeftCS - 1), g, smx);
+  apply_left_strip(X, ldx, cbeg, min(col1, cbeg + kLeftCS - 1), g, smx, flops);
 }
 
 // X <- X H on the row strip [rbeg, rend] (at most kRightRS rows) for every op
@@ -113,7 +116,8 @@ __global__ void __launch_bounds__(kApplyThreads) k_apply_left(double* __restrict
 // Each row's arithmetic is the same for every strip height: RS = 64 for bulk lists, 8 for small
 // critical-path updates (spread over more SMs).
 template <class Geo, int kRightRS = 64>
-__device__ void apply_right_strip(double* __restrict__ X, int ldx, int rbeg, int rend, const Geo& g, double* smx) {
+__device__ void apply_right_strip(double* __restrict__ X, int ldx, int rbeg, int rend, const Geo& g, double* smx,
+                                  unsigned long long* flops = nullptr) {
   double(*Xs)[kRightRS + 1] = reinterpret_cast<double(*)[kRightRS + 1]>(smx);
   double(*Y)[kRightRS + 1] = reinterpret_cast<double(*)[kRightRS + 1]>(smx + kRightCCH * (kRightRS + 1));
   const int t = threadIdx.x;
@@ -125,6 +129,7 @@ __device__ void apply_right_strip(double* __restrict__ X, int ldx, int rbeg, int
     if (ra > rb || op.k <= 0 || op.len <= 0) continue;
     const int h = rb - ra + 1;
     const int k = op.k;
+    if (flops && t == 0) atomicAdd(flops, 4ull * (unsigned long long)op.len * (unsigned long long)k * (unsigned long long)h);
     for (int i = t; i < kMaxK * kRightRS; i += kApplyThreads) Y[i / kRightRS][i % kRightRS] = 0.0;
     // ---- pass 1: Y = X_sub V (h x k) ----
     for (int c0 = 0; c0 < op.len; c0 += kRightCCH) {
@@ -193,11 +198,11 @@ __device__ void apply_right_strip(double* __restrict__ X, int ldx, int rbeg, int
 
 template <class Geo, int kRightRS = 64>
 __global__ void __launch_bounds__(kApplyThreads) k_apply_right(double* __restrict__ X, int ldx, int row0, int row1,
-                                                                Geo g) {
+                                                                Geo g, unsigned long long* flops) {
   extern __shared__ double smx[];
   const int rbeg = row0 + blockIdx.x * kRightRS;
   if (rbeg > row1) return;
-  apply_right_strip<Geo, kRightRS>(X, ldx, rbeg, min(row1, rbeg + kRightRS - 1), g, smx);
+  apply_right_strip<Geo, kRightRS>(X, ldx, rbeg, min(row1, rbeg + kRightRS - 1), g, smx, flops);
 }
 
 constexpr size_t kLeftSmem = sizeof(double) * (size_t)(kLeftRCH + kMaxK) * (kLeftCS + 1);
@@ -205,7 +210,10 @@ template <int RS>
 constexpr size_t right_smem() { return sizeof(double) * (size_t)(kRightCCH + kMaxK) * (RS + 1); }
 
 // Launch helpers: one CTA per strip; the dynamic shared-memory opt-in is set once per
-// instantiation.
+// instantiation.  Under PARAHT_FLAG_KERNEL_TIMES (tl_kclock set) every bulk launch is bracketed
+// by a pair of CUDA events on its stream and counts its algorithmic flops on the device; the
+// 8-row critical-path lists are not timed (they sit on the serial chain, where the events would
+// add to it).
 template <class Geo>
 inline void launch_apply_left(double* X, int ldx, int col0, int col1, const Geo& g, cudaStream_t s) {
   if (col1 < col0) return;
@@ -216,7 +224,13 @@ inline void launch_apply_left(double* X, int ldx, int col0, int col1, const Geo&
   }
   const int nblk = (col1 - col0 + 1 + kLeftCS - 1) / kLeftCS;
   count_launch();
-  k_apply_left<Geo><<<nblk, kApplyThreads, kLeftSmem, s>>>(X, ldx, col0, col1, g);
+  KernelClock* kc = tl_kclock;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  const bool timed = kc && kc->pair(Geo::kSite, &e0, &e1);
+  if (timed) cudaEventRecord(e0, s);
+  k_apply_left<Geo><<<nblk, kApplyThreads, kLeftSmem, s>>>(X, ldx, col0, col1, g,
+                                                           timed ? kc->dflops + Geo::kSite : nullptr);
+  if (timed) cudaEventRecord(e1, s);
 }
 template <class Geo, int RS = 64>
 inline void launch_apply_right(double* X, int ldx, int row0, int row1, const Geo& g, cudaStream_t s) {
@@ -228,7 +242,13 @@ inline void launch_apply_right(double* X, int ldx, int row0, int row1, const Geo
   }
   const int nblk = (row1 - row0 + 1 + RS - 1) / RS;
   count_launch();
-  k_apply_right<Geo, RS><<<nblk, kApplyThreads, right_smem<RS>(), s>>>(X, ldx, row0, row1, g);
+  KernelClock* kc = tl_kclock;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  const bool timed = RS == 64 && kc && kc->pair(Geo::kSite, &e0, &e1);
+  if (timed) cudaEventRecord(e0, s);
+  k_apply_right<Geo, RS><<<nblk, kApplyThreads, right_smem<RS>(), s>>>(X, ldx, row0, row1, g,
+                                                                       timed ? kc->dflops + Geo::kSite : nullptr);
+  if (timed) cudaEventRecord(e1, s);
 }
 
 }  // namespace pht

@@ -30,8 +30,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 TABLE_PATH = os.path.join(HERE, "tune_table.json")
 
 # used when no measured table is present: the reference driver's documented example (r=16,
-# p=8, nq=8) adjusted to the GB300 measurements in profiles/ (p=4 for the single pencil, p r <= 64
-# for the persistent batched kernel)
+# p=8, nq=8) adjusted to what GB300 measurements favour (p=4 for the single pencil, p r <= 64 for
+# the persistent batched kernel)
 FALLBACK = {
     "split": [[1000, 16, 4, 16]],
     "fp64": [[1000, 16, 4, 16]],

@@ -31,3 +31,23 @@ def test_reference_arm_batch_line():
     d = _run("--impl", "reference", "--workload", "batch4096", "--steps", "1", "--warmup", "0")
     assert d["impl"] == "reference" and d["unit"] == "pencils/s" and d["higher_is_better"] is True
     assert d["value"] > 0 and "n log-U" not in d["config"]["workload"]
+
+
+def test_reference_arm_states_its_extrapolation():
+    d = _run("--impl", "reference", "--n", "1200", "--cpu-sample-n", "200", "--steps", "3", "--warmup", "0")
+    assert d["sample_n"] == 200 and d["extrapolated"] is True
+    assert 1 <= d["steps"] <= 3 and d["steps_requested"] == 3
+    assert abs(d["value"] - d["ms_per_step"] / 1e3 * (1200 / 200) ** 3) < 1e-9 * d["value"]
+
+
+def test_budget_plan():
+    sys.path.insert(0, ROOT)
+    import bench
+
+    # the first step always runs; later ones only while a step plus the reserve fits the budget
+    assert bench.budget_plan(100.0, 99.0, 50.0, 0, 20, 10.0)
+    assert bench.budget_plan(1500.0, 400.0, 150.0, 2, 20, 300.0)
+    assert not bench.budget_plan(1500.0, 1100.0, 150.0, 3, 20, 300.0)
+    assert not bench.budget_plan(1500.0, 10.0, 1.0, 20, 20, 0.0)  # all requested steps done
+    args = bench.parse(["--steps", "20", "--warmup", "5"])
+    assert args.budget_s + 0 <= 1700 and args.n == 16000 and args.fp64_params == "32,4,16"
