@@ -183,6 +183,10 @@ extern "C" int paraht_ctx_create(paraht_ctx* out, int device) {
   if (!rc && cudaEventCreateWithFlags(&x.ev_a, cudaEventDisableTiming) != cudaSuccess) rc = PARAHT_ERR_CUDA;
   if (!rc && cudaEventCreateWithFlags(&x.ev_b, cudaEventDisableTiming) != cudaSuccess) rc = PARAHT_ERR_CUDA;
   if (!rc && cudaStreamCreateWithFlags(&x.side2, cudaStreamNonBlocking) != cudaSuccess) rc = PARAHT_ERR_CUDA;
+  if (!rc && cudaStreamCreateWithFlags(&x.side3, cudaStreamNonBlocking) != cudaSuccess) rc = PARAHT_ERR_CUDA;
+  if (!rc && cudaStreamCreateWithFlags(&x.side4, cudaStreamNonBlocking) != cudaSuccess) rc = PARAHT_ERR_CUDA;
+  for (auto& e : x.ev_s2)
+    if (!rc && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) rc = PARAHT_ERR_CUDA;
   for (auto& e : x.ev)
     if (!rc && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) rc = PARAHT_ERR_CUDA;
   if (!rc && cudaMalloc(&x.dstatus, 64) != cudaSuccess) rc = PARAHT_ERR_ALLOC;
@@ -214,10 +218,13 @@ extern "C" int paraht_ctx_destroy(paraht_ctx c) {
     cudaStreamSynchronize(x.side);
     cudaStreamDestroy(x.side);
   }
-  if (x.side2) {
-    cudaStreamSynchronize(x.side2);
-    cudaStreamDestroy(x.side2);
-  }
+  for (cudaStream_t* sp : {&x.side2, &x.side3, &x.side4})
+    if (*sp) {
+      cudaStreamSynchronize(*sp);
+      cudaStreamDestroy(*sp);
+    }
+  for (auto e : x.ev_s2)
+    if (e) cudaEventDestroy(e);
   if (x.bstream) {
     cudaStreamSynchronize(x.bstream);
     cudaStreamDestroy(x.bstream);

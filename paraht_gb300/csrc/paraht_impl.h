@@ -59,7 +59,9 @@ struct Ctx {
   size_t stage_bytes = 0;
   cudaStream_t side = nullptr;      // second stream for work that overlaps the critical path
   cudaStream_t side2 = nullptr;     // third stream (bulk updates that feed nothing on the critical path)
+  cudaStream_t side3 = nullptr, side4 = nullptr;  // stage-2 bulk updates of Q and Z beside those of A, B
   cudaEvent_t ev_a = nullptr, ev_b = nullptr;
+  cudaEvent_t ev_s2[4] = {};        // stage-2 bulk chains: operands prepared, and the joins of A, Q, Z
   cudaEvent_t ev[8] = {};           // stage-1 dependency events
   int sequential_chase = 0;         // 1: run stage-2 sweeps one after the other in one CTA
   long long spin_limit = 1ll << 24;  // polls before a device-side wait gives up

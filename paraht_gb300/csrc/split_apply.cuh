@@ -17,6 +17,17 @@ inline bool split_fits(int k_max, int len_max) { return ws_fits(k_max, len_max);
 // Per-op operand slot of the split-precision kernel.
 typedef WsOpDigits SplitOpData;
 
+// Prepares the split-precision operands of a list in `split_slots` (nothing in FP64, where
+// split_slots is null), so that launches on other streams can apply it with prepare = false once
+// they have waited for this stream.
+template <class Geo>
+inline void prepare_any(void* split_slots, const Geo& g, int nops, cudaStream_t s) {
+  if (split_slots && nops > 0) {
+    count_launch();
+    k_ws_prep<Geo><<<nops, 128, 0, s>>>(g, (WsOpDigits*)split_slots);
+  }
+}
+
 // `split_slots` non-null selects split precision; its `nops` slots receive the prepared operands
 // (prepare = false: they already hold this list's operands, prepared by an earlier call with the
 // same ops on the same stream).

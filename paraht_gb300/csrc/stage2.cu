@@ -76,6 +76,8 @@ int s2_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
   // on the main stream so the phases can be timed separately (the reference inserts taskwaits).
   cudaStream_t sg = ctx.stream;
   cudaStream_t su = (timer || ctx.sequential_chase) ? ctx.stream : ctx.side;
+  const bool one_bulk = timer || ctx.sequential_chase;
+  cudaStream_t sa = one_bulk ? su : ctx.side2, sq = one_bulk ? su : ctx.side3, sz = one_bulk ? su : ctx.side4;
   if (su != sg) {
     cudaEventRecord(ctx.ev_a, sg);
     cudaStreamWaitEvent(su, ctx.ev_a, 0);
@@ -121,17 +123,35 @@ int s2_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
       cudaStreamWaitEvent(su, ctx.ev_a, 0);
     }
     // bulk updates; in the right update a row can lie in block ib's compact-WY range and in
-    // block ib-1's staircase range, so singles and blocks form one ordered list
-    g.kind = kUpRight;
-    apply_right_any(reg[0], B, ldb, 0, n - 1, g, nblocks, su);
-    apply_right_any(reg[0], A, lda, 0, n - 1, g, nblocks, su, false);
-    g.kind = kUpLeft;
-    apply_left_any(reg[1], B, ldb, J, n - 1, g, nblocks, su);
-    apply_left_any(reg[1], A, lda, J, n - 1, g, nblocks, su, false);
-    g.kind = kUpQ;
-    apply_right_any(reg[2], Q, ldq, 0, n - 1, g, nblocks, su);
-    g.kind = kUpZ;
-    apply_right_any(reg[3], Z, ldz, 0, n - 1, g, nblocks, su);
+    // block ib-1's staircase range, so singles and blocks form one ordered list.  The four
+    // matrices are independent: B's right-then-left lists on su, A's on sa, Q's on sq, Z's on sz
+    // (one stream when the phases are timed or the schedule is sequential); each matrix keeps
+    // the reference's order of its own lists (rht2ht.f90:1803-2024).
+    GeoS2 gr = g, gl = g, gq = g, gz = g;
+    gr.kind = kUpRight;
+    gl.kind = kUpLeft;
+    gq.kind = kUpQ;
+    gz.kind = kUpZ;
+    prepare_any(reg[0], gr, nblocks, su);
+    prepare_any(reg[1], gl, nblocks, su);
+    if (su != sa) {
+      cudaEventRecord(ctx.ev_s2[0], su);  // operands of the right and left lists ready
+      cudaStreamWaitEvent(sa, ctx.ev_s2[0], 0);
+      cudaStreamWaitEvent(sq, ctx.ev_a, 0);  // the chase and lookahead of this group are done
+      cudaStreamWaitEvent(sz, ctx.ev_a, 0);
+    }
+    apply_right_any(reg[0], B, ldb, 0, n - 1, gr, nblocks, su, false);
+    apply_left_any(reg[1], B, ldb, J, n - 1, gl, nblocks, su, false);
+    apply_right_any(reg[0], A, lda, 0, n - 1, gr, nblocks, sa, false);
+    apply_left_any(reg[1], A, lda, J, n - 1, gl, nblocks, sa, false);
+    apply_right_any(reg[2], Q, ldq, 0, n - 1, gq, nblocks, sq);
+    apply_right_any(reg[3], Z, ldz, 0, n - 1, gz, nblocks, sz);
+    if (su != sa) {  // join the four chains on su
+      cudaEventRecord(ctx.ev_s2[1], sa);
+      cudaEventRecord(ctx.ev_s2[2], sq);
+      cudaEventRecord(ctx.ev_s2[3], sz);
+      for (int i = 1; i < 4; ++i) cudaStreamWaitEvent(su, ctx.ev_s2[i], 0);
+    }
     if (su != sg) cudaEventRecord(ctx.ev_b, su);
   }
   if (su != sg) cudaStreamWaitEvent(sg, ctx.ev_b, 0);
