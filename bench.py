@@ -96,6 +96,8 @@ def parse(argv=None):
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison step")
     ap.add_argument("--dist", default="std")
     ap.add_argument("--precision", choices=("fp64", "split"), default="split")
+    ap.add_argument("--stage2", choices=("householder", "givens"), default="householder",
+                    help="stage-2 variant: small reflectors (rht2ht_householder) or Givens rotations (rht2ht_givens)")
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--cpu-sample-n", type=int, default=4000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -518,7 +520,8 @@ def run_pencil(args, rank: int, world: int, local: int):
 
     n, r, p, nq = args.n, args.r, args.p, args.nq
     split = args.precision == "split"
-    flags = ph.PARAHT_FLAG_SPLIT if split else 0
+    variant = ph.PARAHT_FLAG_GIVENS if args.stage2 == "givens" else 0
+    flags = (ph.PARAHT_FLAG_SPLIT if split else 0) | variant
     fr, fp, fnq = (int(x) for x in args.fp64_params.split(","))
     do_fp64 = split and not args.no_fp64
     do_check = not args.no_check
@@ -579,14 +582,14 @@ def run_pencil(args, rank: int, world: int, local: int):
     sdev = [torch.from_numpy(np.ascontiguousarray(X.T)).cuda() for X in small0]
     seye = torch.eye(nw, dtype=torch.float64, device="cuda")
     swork = [torch.empty_like(seye) for _ in range(4)]
-    warm_sets = [((r, p, nq), flags)] + ([((fr, fp, fnq), 0)] if do_fp64 else [])
+    warm_sets = [((r, p, nq), flags)] + ([((fr, fp, fnq), variant)] if do_fp64 else [])
     for i in range(max(0, args.warmup - 1)):
         prm, f = warm_sets[i % len(warm_sets)]
         restore(swork, (sdev[0], sdev[1], seye, seye))
         launch(swork, nw, prm, f)
     if do_fp64 and args.warmup < 3:  # the FP64 parameter set gets at least one small warm-up
         restore(swork, (sdev[0], sdev[1], seye, seye))
-        launch(swork, nw, (fr, fp, fnq), 0)
+        launch(swork, nw, (fr, fp, fnq), variant)
     del swork, sdev, seye
     t0w = time.perf_counter()
     if args.warmup > 0:
@@ -608,7 +611,7 @@ def run_pencil(args, rank: int, world: int, local: int):
     with sampler:
         # ---- one FP64 reduction at the FP64 path's own parameters ----
         if do_fp64:
-            t_f = timed((fr, fp, fnq), ph.PARAHT_FLAG_KERNEL_TIMES)
+            t_f = timed((fr, fp, fnq), variant | ph.PARAHT_FLAG_KERNEL_TIMES)
             t_f = job_time(t_f, "cuda")
             fst = ctx.kernel_stats()["stage2"]
             fp64 = {"seconds": t_f, "r": fr, "p": fp, "nq": fnq, "launches": ctx.launch_count(),
@@ -742,8 +745,9 @@ def run_pencil(args, rank: int, world: int, local: int):
             "config": {"workload": (f"stage 2 alone on the saved stage-1 output {args.stage2_from}, n={n}, "
                                     if stage2_only else "") +
                                    f"HT reduction of one pencil n={n} (A N(0,1), B triangular Gaussian R), "
-                                   f"r={r} p={p} nq={nq}, {args.precision}",
+                                   f"r={r} p={p} nq={nq}, {args.precision}, stage 2 {args.stage2}",
                        "n": n, "r": r, "p": p, "nq": nq, "precision": args.precision, "dist": args.dist,
+                       "stage2": args.stage2,
                        "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs 8.2 GB >> L2; pristine input restored between steps outside the timed region",
                        "budget_s": args.budget_s},

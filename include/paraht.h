@@ -58,6 +58,9 @@ extern "C" {
                                          with CUDA events and count its algorithmic work
                                          (paraht_ctx_kernel_stats) */
 
+#define PARAHT_FLAG_GIVENS 128     /* stage 2 by Givens rotations (rht2ht_givens, src/rht2ht.f90:696-1344)
+                                         instead of small reflectors; needs r <= 32 and r + nq <= 64 */
+
 typedef struct paraht_ctx_s* paraht_ctx;
 
 /* ---- context ---- */
@@ -96,6 +99,15 @@ int paraht_rht2ht(int n, double* A, int lda, double* B, int ldb, double* Q, int 
                   int nq, int time_components);
 int paraht_reduce(int n, double* A, int lda, double* B, int ldb, double* Q, int ldq, double* Z, int ldz, int r,
                   int p, int nq, int flags);
+
+/* paraht_rht2ht_givens <-> rht2ht_givens(n, A, lda, B, ldb, Q, ldq, Z, ldz, r, nq)
+ *                          src/rht2ht.f90:696-700 (the reference's stage-2 variant with Givens
+ * rotations: the bulge chase needs no RQ, the rotations of a group are accumulated into
+ * (r+nq) x (r+nq) orthogonal blocks and applied as dense products).  The same H, T as
+ * paraht_rht2ht up to the signs of rows and columns.  r <= 32 and r + nq <= 64, else
+ * PARAHT_ERR_NOT_SUPPORTED.  The device and combined entry points take PARAHT_FLAG_GIVENS. */
+int paraht_rht2ht_givens(int n, double* A, int lda, double* B, int ldb, double* Q, int ldq, double* Z, int ldz, int r,
+                         int nq);
 
 /* Same, on an explicit context (host pointers). */
 int paraht_reduce_host(paraht_ctx ctx, int n, double* A, int lda, double* B, int ldb, double* Q, int ldq, double* Z,
@@ -139,7 +151,8 @@ int paraht_rht2ht_d_noalloc(paraht_ctx ctx, int n, double* A, int lda, double* B
  * those of paraht_reduce_d in FP64 (also when PARAHT_FLAG_SPLIT is set).  The other pencils go
  * through the single-pencil path, largest first, up to eight at a time on internal worker
  * contexts (own streams and workspace), overlapping the persistent launch.
- * PARAHT_FLAG_BATCH_LOOP sends every pencil through paraht_reduce_d (the looped baseline).
+ * PARAHT_FLAG_BATCH_LOOP sends every pencil through paraht_reduce_d (the looped baseline);
+ * PARAHT_FLAG_GIVENS is refused (PARAHT_ERR_NOT_SUPPORTED).
  * Pointers of different pencils must not overlap. ---- */
 #define PARAHT_BATCH_MAX_N 1024
 #define PARAHT_FLAG_BATCH_LOOP 64

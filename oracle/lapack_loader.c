@@ -75,6 +75,8 @@ static int load(void) {
   GET(dlange, "dlange");
   GET(dgghd3, "dgghd3");
   GET(dhgeqz, "dhgeqz");
+  GET(dlartg, "dlartg");
+  GET(drot, "drot");
 #undef GET
   *(void**)(&g_tab.set_num_threads) = sym_threads(h);
   return 1;

@@ -37,6 +37,8 @@ typedef struct {
   void (*dhgeqz)(const char*, const char*, const char*, const lint*, const lint*, const lint*, double*, const lint*, double*,
                  const lint*, double*, double*, double*, double*, const lint*, double*, const lint*, double*, const lint*, lint*,
                  flen, flen, flen);
+  void (*dlartg)(const double*, const double*, double*, double*, double*);
+  void (*drot)(const lint*, double*, const lint*, double*, const lint*, const double*, const double*);
   void (*set_num_threads)(int);
 } lapack_table;
 

@@ -7,6 +7,7 @@ this module.  It restates the reference's Fortran interfaces on numpy arrays
 * ``ab2rht_simple``        -> src/ab2rht.f90:8     (stage 1)
 * ``rht2ht_householder``   -> src/rht2ht.f90:1346  (stage 2, compact WY, lookahead)
 * ``rht2ht_unblocked``     -> src/rht2ht.f90:2053  (stage 2, simple cross-check)
+* ``rht2ht_givens``        -> src/rht2ht.f90:696   (stage 2 with Givens rotations)
 * ``dgghd3``               -> src/profilereduction.f90:156 (LAPACK one-stage baseline)
 * ``backward_error``       -> src/profilereduction.f90:165-174
 """
@@ -32,6 +33,7 @@ def lib():
         L.oracle_ab2rht_simple.argtypes = [i, d, i, d, i, d, i, d, i, i, i, i, d]
         L.oracle_rht2ht_householder.argtypes = [i, d, i, d, i, d, i, d, i, i, i, i, d]
         L.oracle_rht2ht_unblocked.argtypes = [i, d, i, d, i, d, i, d, i, i]
+        L.oracle_rht2ht_givens.argtypes = [i, d, i, d, i, d, i, d, i, i, i]
         L.oracle_dgghd3.argtypes = [i, d, i, d, i, d, i, d, i]
         L.oracle_dgghd3_range.argtypes = [C.c_char, C.c_char, i, i, i, d, i, d, i, d, i, d, i]
         L.oracle_dhgeqz_eigs.argtypes = [i, d, i, d, i, d, d, d]
@@ -92,6 +94,16 @@ def rht2ht_unblocked(A, B, Q, Z, r):
     rc = lib().oracle_rht2ht_unblocked(n, _ptr(A), n, _ptr(B), n, _ptr(Q), n, _ptr(Z), n, int(r))
     if rc != 0:
         raise RuntimeError(f"oracle_rht2ht_unblocked failed: {rc}")
+
+
+def rht2ht_givens(A, B, Q, Z, r, nq):
+    """In-place stage 2 with Givens rotations (src/rht2ht.f90:696-1344)."""
+    _check(A, B, Q, Z)
+    n = A.shape[0]
+    rc = lib().oracle_rht2ht_givens(n, _ptr(A), A.shape[0], _ptr(B), B.shape[0], _ptr(Q), Q.shape[0], _ptr(Z),
+                                    Z.shape[0], int(r), int(nq))
+    if rc != 0:
+        raise RuntimeError(f"oracle_rht2ht_givens failed: {rc}")
 
 
 def dgghd3(A, B, Q, Z):

@@ -828,6 +828,290 @@ int oracle_rht2ht_unblocked(int n, double* A, int lda, double* B, int ldb, doubl
 }
 
 /* ======================================================================================
+ * rht2ht_givens (src/rht2ht.f90:696-1344): stage 2 with Givens rotations.  The bulge chase
+ * reduces each column with nb-1 rotations from the left (dlartg/drot) and removes the single
+ * subdiagonal fill they leave in B with nb-1 rotations from the right, so no RQ is needed; the
+ * rotations of a group are accumulated into (r+nq) x (r+nq) orthogonal matrices U(ib), V(ib)
+ * per block (:970-1003), and the lookahead and delayed updates apply those with dgemm (plus the
+ * staircase rotations that precede a block's full update, :1018-1062, :1246-1274).
+ *
+ * Restated in the reference's task order (mb = 1, so the multi-block branch :1200-1243 is not
+ * taken; a valid schedule of the reference's task graph, whose tasks touch disjoint data or are
+ * ordered by their depend clauses).  The U2/V2/CV2/SV2 copies (:1158-1168) only let generation
+ * k+1 overlap updates k in the reference; run in order, the originals serve.
+ *
+ * Deliberate deviation: the reference's right rotations on B in the lookahead (:1025-1029) and
+ * the delayed update (:1252-1256) run over ig = r-1..1 where the A loops use min(r-1, n-jb-ic);
+ * for the last block of a group that reaches columns beyond n, with the identity rotations
+ * (c = 1, s = 0) left there by the generation.  The oracle uses the A loops' bound for B too:
+ * the rotations skipped are exactly those identities (checked), and no column beyond n is read.
+ * ====================================================================================== */
+static void rot(lint n, double* x, lint incx, double* y, lint incy, double c, double s) {
+  if (n <= 0) return;
+  LP->drot(&n, x, &incx, y, &incy, &c, &s);
+}
+static void lartg(double f, double g, double* c, double* s, double* r) { LP->dlartg(&f, &g, c, s, r); }
+
+int oracle_rht2ht_givens(int n, double* A, int lda, double* B, int ldb, double* Q, int ldq, double* Z, int ldz, int r,
+                         int nq) {
+  if (init_lapack()) return -100;
+  if (n < 3) return 0;
+  const int ldu = r + nq;
+  int nblk0 = (n - 1) / r + ((n - 1) % r != 0);
+  double* U = malloc(sizeof(double) * (size_t)ldu * ldu * nblk0);
+  double* V = malloc(sizeof(double) * (size_t)ldu * ldu * nblk0);
+  double* CU = malloc(sizeof(double) * (size_t)ldu * nq * nblk0);
+  double* SU = malloc(sizeof(double) * (size_t)ldu * nq * nblk0);
+  double* CV = malloc(sizeof(double) * (size_t)ldu * nq * nblk0);
+  double* SV = malloc(sizeof(double) * (size_t)ldu * nq * nblk0);
+  double* work = malloc(sizeof(double) * (size_t)(r + nq) * n);
+  if (!U || !V || !CU || !SU || !CV || !SV || !work) return -101;
+  const double one = 1.0, zero = 0.0;
+  int bad_skip = 0;
+#define RX(M, i, ic, ib) (M)[((size_t)(i)-1) + ((size_t)(ic)-1) * ldu + ((size_t)(ib)-1) * ldu * nq]
+#define GX(M, i, j, ib) (M)[((size_t)(i)-1) + ((size_t)(j)-1) * ldu + ((size_t)(ib)-1) * ldu * ldu]
+  lint lu = ldu;
+  for (int jblock = 1; jblock <= n - 2; jblock += nq) { /* :766 */
+    const int nblocks = (n - jblock) / r + ((n - jblock) % r != 0);
+    /* ---- generation: rotations, updating only a band of A and B (:776-960) ---- */
+    for (size_t e = 0; e < (size_t)ldu * nq * nblk0; e++) {
+      CU[e] = 1.0;
+      CV[e] = 1.0;
+      SU[e] = 0.0;
+      SV[e] = 0.0;
+    }
+    for (int ic = 1; ic <= nq; ic++) {
+      const int jc = jblock + ic - 1;
+      int nb = MIN(r, n - jc);
+      int istart = jblock + 1;
+      if (jc + r <= n) /* :806-814 */
+        for (int i = 1; i <= ic - 1; i++)
+          for (int ig = r - 1; ig >= 1; ig--)
+            rot(1, &Bx(jblock + i - 1 + ig, jc + r), ldb, &Bx(jblock + i + ig, jc + r), ldb, RX(CU, i + ig - 1, i, 1),
+                RX(SU, i + ig - 1, i, 1));
+      for (int i = 1; i <= ic - 1; i++) /* :820-828 */
+        if (jc <= n)
+          for (int ig = MIN(r - 1, n - (jblock + i)); ig >= 1; ig--)
+            rot(1, &Ax(jblock + i - 1 + ig, jc), lda, &Ax(jblock + i + ig, jc), lda, RX(CU, i + ig - 1, i, 1),
+                RX(SU, i + ig - 1, i, 1));
+      if (nb < 2) continue;
+      double temp;
+      for (int ig = nb - 1; ig >= 1; ig--) { /* :833-838 */
+        lartg(Ax(jc + ig, jc), Ax(jc + ig + 1, jc), &RX(CU, ic + ig - 1, ic, 1), &RX(SU, ic + ig - 1, ic, 1), &temp);
+        Ax(jc + ig, jc) = temp;
+        Ax(jc + ig + 1, jc) = 0.0;
+      }
+      for (int ig = nb - 1; ig >= 1; ig--) /* :840-843 */
+        rot(nb, &Bx(jc + ig, jc + 1), ldb, &Bx(jc + ig + 1, jc + 1), ldb, RX(CU, ic + ig - 1, ic, 1),
+            RX(SU, ic + ig - 1, ic, 1));
+      for (int ig = nb - 1; ig >= 1; ig--) { /* :846-854 */
+        lartg(Bx(jc + ig + 1, jc + ig + 1), Bx(jc + ig + 1, jc + ig), &RX(CV, ic + ig - 1, ic, 1),
+              &RX(SV, ic + ig - 1, ic, 1), &temp);
+        Bx(jc + ig + 1, jc + ig + 1) = temp;
+        Bx(jc + ig + 1, jc + ig) = 0.0;
+        rot(ig, &Bx(jc + 1, jc + ig + 1), 1, &Bx(jc + 1, jc + ig), 1, RX(CV, ic + ig - 1, ic, 1),
+            RX(SV, ic + ig - 1, ic, 1));
+      }
+      for (int ig = nb - 1; ig >= 1; ig--) /* :856-859 */
+        rot(MIN(n, jc + r + nb) - jc, &Ax(jc + 1, jc + ig + 1), 1, &Ax(jc + 1, jc + ig), 1,
+            RX(CV, ic + ig - 1, ic, 1), RX(SV, ic + ig - 1, ic, 1));
+      for (int ig = nb - 1; ig >= 1; ig--) /* :862-865 */
+        rot(jc - istart + 1, &Bx(istart, jc + ig + 1), 1, &Bx(istart, jc + ig), 1, RX(CV, ic + ig - 1, ic, 1),
+            RX(SV, ic + ig - 1, ic, 1));
+      for (int ig = nb - 1; ig >= 1; ig--) /* :867-870 */
+        rot(jc - istart + 1, &Ax(istart, jc + ig + 1), 1, &Ax(istart, jc + ig), 1, RX(CV, ic + ig - 1, ic, 1),
+            RX(SV, ic + ig - 1, ic, 1));
+      for (int jb = jc + 1; jb <= n; jb += r) { /* :879 chase the fill down */
+        const int ib = (jb - (jc + 1)) / r + 2;
+        nb = MIN(r, n - jb - r + 1);
+        istart = MAX(jblock + 1, jblock + 1 + (ib - 1) * r - (nq - ic) * r);
+        if (jb + r + r - 1 <= n) /* :892-900 */
+          for (int i = 1; i <= ic - 1; i++)
+            for (int ig = r - 1; ig >= 1; ig--)
+              rot(1, &Bx(jb + r - ic + i + ig - 1, jb + r + r - 1), ldb, &Bx(jb + r - ic + i + ig, jb + r + r - 1), ldb,
+                  RX(CU, i + ig - 1, i, ib), RX(SU, i + ig - 1, i, ib));
+        for (int i = 1; i <= ic - 1; i++) /* :906-914 */
+          if (jb + r - ic + i <= n)
+            for (int ig = MIN(r, n - (jb + r - ic + i) + 1) - 1; ig >= 1; ig--)
+              rot(1, &Ax(jb + r - ic + i + ig - 1, jb), lda, &Ax(jb + r - ic + i + ig, jb), lda,
+                  RX(CU, i + ig - 1, i, ib), RX(SU, i + ig - 1, i, ib));
+        if (nb < 2) continue;
+        for (int ig = nb - 1; ig >= 1; ig--) { /* :919-924 */
+          lartg(Ax(jb + r - 1 + ig, jb), Ax(jb + r + ig, jb), &RX(CU, ic + ig - 1, ic, ib), &RX(SU, ic + ig - 1, ic, ib),
+                &temp);
+          Ax(jb + ig + r - 1, jb) = temp;
+          Ax(jb + ig + r, jb) = 0.0;
+        }
+        for (int ig = nb - 1; ig >= 1; ig--) /* :926-929 */
+          rot(nb, &Bx(jb + r - 1 + ig, jb + r), ldb, &Bx(jb + ig + r, jb + r), ldb, RX(CU, ic + ig - 1, ic, ib),
+              RX(SU, ic + ig - 1, ic, ib));
+        for (int ig = nb - 1; ig >= 1; ig--) { /* :932-940 */
+          lartg(Bx(jb + r + ig, jb + r + ig), Bx(jb + r + ig, jb + r + ig - 1), &RX(CV, ic + ig - 1, ic, ib),
+                &RX(SV, ic + ig - 1, ic, ib), &temp);
+          Bx(jb + r + ig, jb + r + ig) = temp;
+          Bx(jb + r + ig, jb + r + ig - 1) = 0.0;
+          rot(ig, &Bx(jb + r, jb + r + ig), 1, &Bx(jb + r, jb + r + ig - 1), 1, RX(CV, ic + ig - 1, ic, ib),
+              RX(SV, ic + ig - 1, ic, ib));
+        }
+        for (int ig = nb - 1; ig >= 1; ig--) /* :942-945 */
+          rot(MIN(n, jb + 2 * r + nb - 1) - (jb + r) + 1, &Ax(jb + r, jb + r + ig), 1, &Ax(jb + r, jb + r + ig - 1), 1,
+              RX(CV, ic + ig - 1, ic, ib), RX(SV, ic + ig - 1, ic, ib));
+        for (int ig = nb - 1; ig >= 1; ig--) /* :948-951 */
+          rot(jb + r - istart, &Bx(istart, jb + r + ig), 1, &Bx(istart, jb + r + ig - 1), 1,
+              RX(CV, ic + ig - 1, ic, ib), RX(SV, ic + ig - 1, ic, ib));
+        for (int ig = nb - 1; ig >= 1; ig--) /* :953-956 */
+          rot(jb + r - istart, &Ax(istart, jb + r + ig), 1, &Ax(istart, jb + r + ig - 1), 1,
+              RX(CV, ic + ig - 1, ic, ib), RX(SV, ic + ig - 1, ic, ib));
+      }
+    }
+    /* ---- accumulate the rotations into U(ib), V(ib) (:970-1003) ---- */
+    for (int ib = 1; ib <= nblocks; ib++) {
+      LP->dlaset("A", &lu, &lu, &zero, &one, &GX(U, 1, 1, ib), &lu, 1);
+      for (int ic = 1; ic <= nq; ic++)
+        for (int ig = r - 1; ig >= 1; ig--)
+          rot(ldu, &GX(U, 1, ic - 1 + ig, ib), 1, &GX(U, 1, ic + ig, ib), 1, RX(CU, ic + ig - 1, ic, ib),
+              RX(SU, ic + ig - 1, ic, ib));
+      LP->dlaset("A", &lu, &lu, &zero, &one, &GX(V, 1, 1, ib), &lu, 1);
+      for (int ic = 1; ic <= nq; ic++)
+        for (int ig = r - 1; ig >= 1; ig--)
+          rot(ldu, &GX(V, 1, ic + ig, ib), 1, &GX(V, 1, ic + ig - 1, ib), 1, RX(CV, ic + ig - 1, ic, ib),
+              RX(SV, ic + ig - 1, ic, ib));
+    }
+    /* right rotations of block ib on rows [lo, hi) of X (the lookahead :1018-1029, :1074-1087
+     * and the delayed update's staircase :1246-1257, :1289-1296); columns beyond n are not touched */
+#define STAIR(X, ldx, ib, lo_of_ic, hi_of_ic)                                                              \
+  do {                                                                                                     \
+    const int jb_ = jblock + ((ib)-1) * r;                                                                 \
+    for (int ic = 1; ic <= nq; ic++) {                                                                     \
+      const int lo_ = (lo_of_ic), hi_ = (hi_of_ic);                                                        \
+      if (hi_ <= lo_) continue;                                                                            \
+      for (int ig = r - 1; ig >= 1; ig--) {                                                                \
+        if (jb_ + ic + ig > n) {                                                                           \
+          if (RX(CV, ic + ig - 1, ic, (ib)) != 1.0 || RX(SV, ic + ig - 1, ic, (ib)) != 0.0) bad_skip = 1; \
+          continue;                                                                                        \
+        }                                                                                                  \
+        rot(hi_ - lo_, &IX(X, ldx, lo_, jb_ + ic + ig), 1, &IX(X, ldx, lo_, jb_ + ic + ig - 1), 1,         \
+            RX(CV, ic + ig - 1, ic, (ib)), RX(SV, ic + ig - 1, ic, (ib)));                                 \
+      }                                                                                                    \
+    }                                                                                                      \
+  } while (0)
+    /* ---- lookahead on B (:1008-1049) ---- */
+    for (int ib = nblocks; ib >= 1; ib--)
+      STAIR(B, ldb, ib, MAX(jblock + 1, jblock + 1 + (ib - 1) * r - nq * r - (nq - ic) * r),
+            MAX(jblock + 1, jblock + 1 + (ib - 1) * r - (nq - ic) * r));
+    for (int ib = nblocks; ib >= 1; ib--) {
+      const int jb = jblock + (ib - 1) * r, nb = MIN(n - jb, r + nq);
+      const int istop = MIN(n, jblock + (ib - 1) * r + r + nq - 1);
+      const int istop2 = MIN(n, jblock + (ib - 1) * r + r + nq + r * nq - 1);
+      if (istop2 > istop) {
+        lint m = nb, nn = istop2 - istop, lw = nb, lb = ldb;
+        LP->dgemm("T", "N", &m, &nn, &m, &one, &GX(U, 1, 1, ib), &lu, &Bx(jb + 1, istop + 1), &lb, &zero, work, &lw, 1,
+                  1);
+        lacpy(nb, istop2 - istop, work, nb, &Bx(jb + 1, istop + 1), ldb);
+      }
+    }
+    /* ---- lookahead on A (:1065-1131) ---- */
+    for (int ib = nblocks; ib >= 1; ib--)
+      STAIR(A, lda, ib, MAX(jblock + 1, jblock + 1 + (ib - 1) * r - nq * r - (nq - ic) * r),
+            MAX(jblock + 1, jblock + 1 + (ib - 1) * r - (nq - ic) * r));
+    for (int ib = nblocks; ib >= 1; ib--) {
+      int jb, nb, row0;
+      if (ib == 1) {
+        jb = jblock;
+        nb = MIN(n - jb, r + nq);
+        row0 = jb + 1;
+      } else {
+        jb = jblock + 1 + (ib - 2) * r;
+        nb = MIN(n - jb - r + 1, r + nq);
+        row0 = jb + r;
+      }
+      const int istop = MIN(n, jb + nq - 1);
+      const int istop2 = MIN(n, jblock + (ib - 1) * r + r + nq + r * nq - 1);
+      if (istop2 > istop && nb > 0) {
+        lint m = nb, nn = istop2 - istop, lw = nb, la = lda;
+        LP->dgemm("T", "N", &m, &nn, &m, &one, &GX(U, 1, 1, ib), &lu, &Ax(row0, istop + 1), &la, &zero, work, &lw, 1,
+                  1);
+        lacpy(nb, istop2 - istop, work, nb, &Ax(row0, istop + 1), lda);
+      }
+    }
+    /* ---- delayed update of B (:1173-1283): right (staircase rotations, then dgemm on rows
+     * 1..istart-1), then left ---- */
+    for (int ib = nblocks; ib >= 1; ib--) {
+      const int jb = jblock + (ib - 1) * r, nb = MIN(n - jb, r + nq);
+      const int istart = MAX(jblock + 1, jblock + 1 + (ib - 1) * r - (2 * nq - 1) * r);
+      STAIR(B, ldb, ib, istart, MAX(jblock + 1, jblock + 1 + (ib - 1) * r - nq * r - (nq - ic) * r));
+      if (istart - 1 >= 1) {
+        lint m = istart - 1, nn = nb, lb = ldb, lw = istart - 1;
+        LP->dgemm("N", "N", &m, &nn, &nn, &one, &Bx(1, jb + 1), &lb, &GX(V, 1, 1, ib), &lu, &zero, work, &lw, 1, 1);
+        lacpy(istart - 1, nb, work, istart - 1, &Bx(1, jb + 1), ldb);
+      }
+    }
+    for (int ib = nblocks; ib >= 1; ib--) {
+      const int jb = jblock + (ib - 1) * r, nb = MIN(n - jb, r + nq);
+      const int istop = MIN(n, jblock + (ib - 1) * r + r + nq + r * nq - 1);
+      if (n > istop) {
+        lint m = nb, nn = n - istop, lw = nb, lb = ldb;
+        LP->dgemm("T", "N", &m, &nn, &m, &one, &GX(U, 1, 1, ib), &lu, &Bx(jb + 1, istop + 1), &lb, &zero, work, &lw, 1,
+                  1);
+        lacpy(nb, n - istop, work, nb, &Bx(jb + 1, istop + 1), ldb);
+      }
+    }
+    /* ---- delayed update of A (:1290-1334) ---- */
+    for (int ib = nblocks; ib >= 1; ib--) {
+      const int jb = jblock + (ib - 1) * r, nb = MIN(n - jb, r + nq);
+      const int istart = MAX(jblock + 1, jblock + 1 + (ib - 1) * r - (2 * nq - 1) * r);
+      STAIR(A, lda, ib, istart, MAX(jblock + 1, jblock + 1 + (ib - 1) * r - (2 * nq - ic) * r));
+      if (istart - 1 >= 1) {
+        lint m = istart - 1, nn = nb, la = lda, lw = istart - 1;
+        LP->dgemm("N", "N", &m, &nn, &nn, &one, &Ax(1, jb + 1), &la, &GX(V, 1, 1, ib), &lu, &zero, work, &lw, 1, 1);
+        lacpy(istart - 1, nb, work, istart - 1, &Ax(1, jb + 1), lda);
+      }
+    }
+    for (int ib = nblocks; ib >= 1; ib--) {
+      int jb, nb, row0;
+      if (ib == 1) {
+        jb = jblock;
+        nb = MIN(n - jb, r + nq);
+        row0 = jb + 1;
+      } else {
+        jb = jblock + 1 + (ib - 2) * r;
+        nb = MIN(n - jb - r + 1, r + nq);
+        row0 = jb + r;
+      }
+      const int istop = MIN(n, jblock + (ib - 1) * r + r + nq + r * nq - 1);
+      if (n > istop && nb > 0) {
+        lint m = nb, nn = n - istop, lw = nb, la = lda;
+        LP->dgemm("T", "N", &m, &nn, &m, &one, &GX(U, 1, 1, ib), &lu, &Ax(row0, istop + 1), &la, &zero, work, &lw, 1,
+                  1);
+        lacpy(nb, n - istop, work, nb, &Ax(row0, istop + 1), lda);
+      }
+    }
+    /* ---- Q and Z (:1340-1366 of the task list: Q(:, jb+1:jb+nb) <- Q(:, ...) U(ib)) ---- */
+    for (int ib = nblocks; ib >= 1; ib--) {
+      const int jb = jblock + (ib - 1) * r, nb = MIN(n - jb, r + nq);
+      lint m = n, nn = nb, lqq = ldq, lzz = ldz, lw = n;
+      LP->dgemm("N", "N", &m, &nn, &nn, &one, &IX(Q, ldq, 1, jb + 1), &lqq, &GX(U, 1, 1, ib), &lu, &zero, work, &lw, 1,
+                1);
+      lacpy(n, nb, work, n, &IX(Q, ldq, 1, jb + 1), ldq);
+      LP->dgemm("N", "N", &m, &nn, &nn, &one, &IX(Z, ldz, 1, jb + 1), &lzz, &GX(V, 1, 1, ib), &lu, &zero, work, &lw, 1,
+                1);
+      lacpy(n, nb, work, n, &IX(Z, ldz, 1, jb + 1), ldz);
+    }
+#undef STAIR
+  }
+#undef RX
+#undef GX
+  free(U);
+  free(V);
+  free(CU);
+  free(SU);
+  free(CV);
+  free(SV);
+  free(work);
+  return bad_skip ? -102 : 0;
+}
+
+/* ======================================================================================
  * LAPACK baselines and checks used by the reference driver (src/profilereduction.f90).
  * ====================================================================================== */
 

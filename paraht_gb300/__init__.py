@@ -6,6 +6,8 @@ Python mirror of the reference's Fortran interface (same names, argument order a
       src/ab2rht.f90:8 -- stage 1, (A, B) -> (r-Hessenberg, triangular)
 * ``rht2ht_householder(n, A, lda, B, ldb, Q, ldq, Z, ldz, r, nq, time_components)``
       src/rht2ht.f90:1346 -- stage 2, r-Hessenberg -> Hessenberg
+* ``rht2ht_givens(n, A, lda, B, ldb, Q, ldq, Z, ldz, r, nq)``
+      src/rht2ht.f90:696 -- stage 2 with Givens rotations (the reference's other stage-2 variant)
 
 Arrays are numpy float64 in Fortran (column-major) order and are overwritten in place; Q and Z
 are accumulated (right-multiplied), as in the reference.  The work runs on the GPU through
@@ -22,14 +24,15 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import (PARAHT_BATCH_MAX_N, PARAHT_FLAG_BATCH_LOOP, PARAHT_FLAG_CHECK_FINITE, PARAHT_FLAG_KERNEL_TIMES,
-                   PARAHT_FLAG_NO_ZERO_FILL, PARAHT_FLAG_SEQUENTIAL, PARAHT_FLAG_SPLIT, PARAHT_FLAG_TIME_COMPONENTS,
-                   ParahtError, check, lib)
+from ._lib import (PARAHT_BATCH_MAX_N, PARAHT_FLAG_BATCH_LOOP, PARAHT_FLAG_CHECK_FINITE, PARAHT_FLAG_GIVENS,
+                   PARAHT_FLAG_KERNEL_TIMES, PARAHT_FLAG_NO_ZERO_FILL, PARAHT_FLAG_SEQUENTIAL, PARAHT_FLAG_SPLIT,
+                   PARAHT_FLAG_TIME_COMPONENTS, ParahtError, check, lib)
 
 __all__ = [
-    "ab2rht_simple", "rht2ht_householder", "reduce", "ht", "gghd3", "Context", "ParahtError",
+    "ab2rht_simple", "rht2ht_householder", "rht2ht_givens", "reduce", "ht", "gghd3", "Context", "ParahtError",
     "PARAHT_FLAG_TIME_COMPONENTS", "PARAHT_FLAG_CHECK_FINITE", "PARAHT_FLAG_SPLIT", "PARAHT_FLAG_NO_ZERO_FILL",
-    "PARAHT_FLAG_SEQUENTIAL", "PARAHT_FLAG_KERNEL_TIMES", "PARAHT_FLAG_BATCH_LOOP", "PARAHT_BATCH_MAX_N",
+    "PARAHT_FLAG_SEQUENTIAL", "PARAHT_FLAG_KERNEL_TIMES", "PARAHT_FLAG_BATCH_LOOP", "PARAHT_FLAG_GIVENS",
+    "PARAHT_BATCH_MAX_N",
 ]
 
 PHASE_NAMES = ("s1_genleft", "s1_genright", "s1_mul", "s2_gen", "s2_lookahead", "s2_application", "copies", "total")
@@ -56,6 +59,13 @@ def rht2ht_householder(n, A, lda, B, ldb, Q, ldq, Z, ldz, r, nq, time_components
     check(lib().paraht_rht2ht(int(n), _host_ptr(A), int(lda), _host_ptr(B), int(ldb), _host_ptr(Q), int(ldq),
                               _host_ptr(Z), int(ldz), int(r), int(nq), int(bool(time_components))),
           "rht2ht_householder")
+
+
+def rht2ht_givens(n, A, lda, B, ldb, Q, ldq, Z, ldz, r, nq):
+    """Stage 2 with Givens rotations (src/rht2ht.f90:696-700), in place on host arrays; the same
+    H, T as rht2ht_householder up to row/column signs.  Needs r <= 32 and r + nq <= 64."""
+    check(lib().paraht_rht2ht_givens(int(n), _host_ptr(A), int(lda), _host_ptr(B), int(ldb), _host_ptr(Q), int(ldq),
+                                     _host_ptr(Z), int(ldz), int(r), int(nq)), "rht2ht_givens")
 
 
 def reduce(A, B, Q, Z, r, p, nq, flags=0):

@@ -17,6 +17,7 @@ PARAHT_FLAG_NO_ZERO_FILL = 8
 PARAHT_FLAG_SEQUENTIAL = 16
 PARAHT_FLAG_KERNEL_TIMES = 32
 PARAHT_FLAG_BATCH_LOOP = 64
+PARAHT_FLAG_GIVENS = 128
 PARAHT_BATCH_MAX_N = 1024
 
 ERRORS = {
@@ -43,6 +44,7 @@ SIGNATURES = {
     "paraht_ab2rht": [_i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i, _i],
     "paraht_rht2ht": [_i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i, _i],
     "paraht_reduce": [_i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i, _i, _i],
+    "paraht_rht2ht_givens": [_i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i],
     "paraht_reduce_host": [C.c_void_p, _i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i, _i, _i],
     "paraht_ab2rht_d": [C.c_void_p, _i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i, _i],
     "paraht_rht2ht_d": [C.c_void_p, _i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i, _i],

@@ -20,7 +20,7 @@ LIB = os.path.join(BUILD, "libparaht.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"] + ARCH
 # Per-file flags: the pipelined chase reads data other CTAs wrote, so its global loads bypass L1.
-FILE_FLAGS = {"stage2_chase.cu": ["-Xptxas", "-dlcm=cg"]}
+FILE_FLAGS = {"stage2_chase.cu": ["-Xptxas", "-dlcm=cg"], "stage2g_chase.cu": ["-Xptxas", "-dlcm=cg"]}
 
 
 def nvcc() -> str:

@@ -371,7 +371,9 @@ static int run_device(Ctx& x, int which, int n, double* A, int lda, double* B, i
   }
   if (!rc && (which & 2)) {
     x.timer.reset(3);
-    rc = pht::s2_run(x, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, nq, timed ? &x.timer : nullptr);
+    rc = (flags & PARAHT_FLAG_GIVENS)
+             ? pht::s2g_run(x, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, nq, timed ? &x.timer : nullptr)
+             : pht::s2_run(x, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, nq, timed ? &x.timer : nullptr);
     if (!rc && timed) {
       rc = finish(x);
       x.timer.accumulate(x.phase, 8);
@@ -587,6 +589,16 @@ extern "C" int paraht_rht2ht(int n, double* A, int lda, double* B, int ldb, doub
   return host_entry(c, 0, 2, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, 2, nq,
                     time_components ? PARAHT_FLAG_TIME_COMPONENTS : 0);
 }
+extern "C" int paraht_rht2ht_givens(int n, double* A, int lda, double* B, int ldb, double* Q, int ldq, double* Z,
+                                    int ldz, int r, int nq) {
+  if (const int bad = check_args(2, 0, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, 2, nq)) return bad;
+  if (n == 0) return 0;
+  if (!pht::s2g_supported(r, nq)) return PARAHT_ERR_NOT_SUPPORTED;
+  paraht_ctx c;
+  const int rc = default_ctx(&c);
+  if (rc) return rc;
+  return host_entry(c, 0, 2, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, 2, nq, PARAHT_FLAG_GIVENS);
+}
 extern "C" int paraht_reduce(int n, double* A, int lda, double* B, int ldb, double* Q, int ldq, double* Z, int ldz,
                              int r, int p, int nq, int flags) {
   if (const int bad = check_args(3, 0, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, p, nq)) return bad;
@@ -603,6 +615,7 @@ extern "C" int paraht_reduce_batched_d(paraht_ctx c, int count, const int* n, do
                                        int flags) {
   if (!ctx_ok(c)) return PARAHT_ERR_BAD_CTX;
   if (count < 0) return -2;
+  if (flags & PARAHT_FLAG_GIVENS) return PARAHT_ERR_NOT_SUPPORTED;  // the persistent kernel chases with reflectors
   if (count > 0 && (!n || !A || !lda || !B || !ldb || !Q || !ldq || !Z || !ldz || !r || !p || !nq)) return -3;
   for (int i = 0; i < count; ++i) {
     const int rc = check_args(3, 0, n[i], A[i], lda[i], B[i], ldb[i], Q[i], ldq[i], Z[i], ldz[i], r[i], p[i], nq[i]);

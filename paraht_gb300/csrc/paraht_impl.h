@@ -108,6 +108,11 @@ int s1_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
            int p, PhaseTimer* timer);
 int s2_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, int ldq, double* Z, int ldz, int r,
            int nq, PhaseTimer* timer);
+// Stage 2 with Givens rotations (stage2g.cu); supported for r <= 32, r + nq <= 64.
+size_t s2g_workspace_bytes(int n, int r, int nq);
+bool s2g_supported(int r, int nq);
+int s2g_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, int ldq, double* Z, int ldz, int r,
+            int nq, PhaseTimer* timer);
 // Zeroes entries below the structure (lower bandwidth `band` for A, 0 for B) and records the
 // largest absolute value zeroed in dres[0] (A) and dres[1] (B).
 void zero_fill(cudaStream_t s, int n, double* A, int lda, int band, double* B, int ldb, double* dres);

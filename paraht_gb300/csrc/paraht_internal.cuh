@@ -88,7 +88,18 @@ struct WYOp {
   int ldv;
   const double* T;  // k x k, column-major, leading dimension ldt
   int ldt;
+  // dense = 1: the op is C <- C G (right) / C <- G^T C (left) for an accumulated orthogonal
+  // len x len block G (the Givens stage 2); it is stored as V = I (len x len) and T = I - G
+  // (k = len), the same product C - C V T V^T, and its algorithmic work is 2 len^2 flops per
+  // row instead of 4 len k
+  int dense = 0;
 };
+
+// Algorithmic flops of an op per strip row (per column for left ops).
+PHT_DEV unsigned long long op_row_flops(const WYOp& w) {
+  return w.dense ? 2ull * (unsigned long long)w.len * (unsigned long long)w.len
+                 : 4ull * (unsigned long long)w.len * (unsigned long long)w.k;
+}
 
 }  // namespace pht
 

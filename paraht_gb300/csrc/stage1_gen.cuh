@@ -405,27 +405,30 @@ static __device__ void s1_rgen_body(const double* __restrict__ B, int ldb, const
     }
     __syncthreads();
     // ---- LQ (dgelq2) of M: reflector i from row i, columns i..nb2-1; same lane layout ----
+    // M's rows are orthonormal (the first nb rows of an orthogonal matrix), so the LQ needs no
+    // norms or dot products (Householder reconstruction from an orthonormal basis, Ballard et al.
+    // 2014): after reflectors 0..i-1, row i is zero before column i and has unit norm, so
+    // DLARFG gives |beta| = 1, tau = 1 + |alpha|, scal = sign(alpha) / (1 + |alpha|); every
+    // later row r is orthogonal to row i, so its dot product with the reflector tail is
+    // -alpha M[r][i] and the update of row r reduces to M[r][c] -= (scal M[r][i]) M[i][c].  The
+    // entries M[r][i] this leaves (r > i, DLARFG's L factor, zero up to rounding) are never read.
+    // A tail that is exactly zero takes tau = 0 (H = I), as in DLARFG.
     for (int i = 0; i < nb; ++i) {
-      double s = 0.0;
-      if (r >= i && r < nb)
-        for (int cc = i + 1 + part; cc < nb2; cc += QM) s = fma(M[r * ldm + cc], M[i * ldm + cc], s);
-      for (int off = 1; off < QM; off <<= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-      if (r == i && part == 0) {
-        dvec[r] = s;
-        const Reflector h = reflector_from_norm2(M[i * ldm + i], s);
-        sc[0] = h.tau;
-        sc[1] = h.scal;
-        sc[2] = h.beta;
-      } else if (part == 0 && r > i && r < nb) {
-        dvec[r] = s;
-      }
-      __syncthreads();
-      const double tl = sc[0], scal = sc[1], beta = sc[2];
-      if (r > i && r < nb && tl != 0.0) {
-        const double w = M[r * ldm + i] + scal * dvec[r];
-        const double tw = tl * w, tws = tw * scal;
-        for (int cc = i + 1 + part; cc < nb2; cc += QM) M[r * ldm + cc] = fma(-tws, M[i * ldm + cc], M[r * ldm + cc]);
-        if (part == 0) M[r * ldm + i] -= tw;
+      bool nz = false;
+      if (r == i)
+        for (int cc = i + 1 + part; cc < nb2; cc += QM) nz |= M[i * ldm + cc] != 0.0;
+      const bool any = __syncthreads_or(nz) != 0;  // also publishes the previous step's rows
+      const double alpha = M[i * ldm + i];
+      double tl = 0.0, scal = 1.0, beta = alpha;
+      if (any) {
+        const double aa = fabs(alpha);
+        tl = 1.0 + aa;
+        scal = copysign(1.0 / tl, alpha);
+        beta = -copysign(1.0, alpha);
+        if (r > i && r < nb) {
+          const double tws = M[r * ldm + i] * scal;
+          for (int cc = i + 1 + part; cc < nb2; cc += QM) M[r * ldm + cc] = fma(-tws, M[i * ldm + cc], M[r * ldm + cc]);
+        }
       }
       __syncthreads();
       if (r == i) {
@@ -435,8 +438,8 @@ static __device__ void s1_rgen_body(const double* __restrict__ B, int ldb, const
           tauL[i] = tl;
         }
       }
-      __syncthreads();
     }
+    __syncthreads();
     // VRc[c][i] = VR[i][c]: 1 at c == i, M[i][c] for c > i, 0 before
     for (int e = t; e < L * nb; e += blockDim.x) {
       const int cc = e % L, i = e / L;

@@ -35,7 +35,7 @@ __device__ void apply_left_strip(double* __restrict__ X, int ldx, int cbeg, int 
     if (ca > cb || op.k <= 0 || op.len <= 0) continue;
     const int w = cb - ca + 1;
     const int k = op.k;
-    if (flops && t == 0) atomicAdd(flops, 4ull * (unsigned long long)op.len * (unsigned long long)k * (unsigned long long)w);
+    if (flops && t == 0) atomicAdd(flops, op_row_flops(op) * (unsigned long long)w);
     // ---- pass 1: W = V^T X_sub (k x w) ----
     for (int i = t; i < kMaxK * kLeftCS; i += kApplyThreads) W[i / kLeftCS][i % kLeftCS] = 0.0;
     for (int r0 = 0; r0 < op.len; r0 += kLeftRCH) {
@@ -129,7 +129,7 @@ __device__ void apply_right_strip(double* __restrict__ X, int ldx, int rbeg, int
     if (ra > rb || op.k <= 0 || op.len <= 0) continue;
     const int h = rb - ra + 1;
     const int k = op.k;
-    if (flops && t == 0) atomicAdd(flops, 4ull * (unsigned long long)op.len * (unsigned long long)k * (unsigned long long)h);
+    if (flops && t == 0) atomicAdd(flops, op_row_flops(op) * (unsigned long long)h);
     for (int i = t; i < kMaxK * kRightRS; i += kApplyThreads) Y[i / kRightRS][i % kRightRS] = 0.0;
     // ---- pass 1: Y = X_sub V (h x k) ----
     for (int c0 = 0; c0 < op.len; c0 += kRightCCH) {

@@ -209,6 +209,31 @@ __global__ void __launch_bounds__(128) k_ws_prep(Geo g, WsOpDigits* out) {
   const bool live = op.len > 0 && op.k > 0;
   const int len = live ? op.len : 0, k = live ? op.k : 0;
   const bool two = !g.masks_y();
+  if (op.dense) {
+    // C -= C M with M = T = I - G given explicitly (len <= kWsMM, one-product form only)
+    for (int e = t; e < kWsMM * kWsMM; e += 128) {
+      const int ci = e % kWsMM, co = e / kWsMM;
+      Msh[ci][co] = (ci < len && co < len) ? op.T[ci + (size_t)co * op.ldt] : 0.0;
+    }
+    __syncthreads();
+    {  // scales of M's columns: 4 lanes per column
+      const int co = t >> 2, part = t & 3;
+      uint64_t amax = 0;
+      for (int c = part; c < kWsMM; c += 4) amax = max(amax, ws_abs_bits(Msh[c][co]));
+      amax = max(amax, (uint64_t)__shfl_xor_sync(0xffffffffu, (long long)amax, 1));
+      amax = max(amax, (uint64_t)__shfl_xor_sync(0xffffffffu, (long long)amax, 2));
+      if (part == 0) {
+        D->fm[co] = ws_exp_bits(amax);
+        sc[co] = ws_exp_bits(amax);
+      }
+    }
+    __syncthreads();
+    for (int e = t; e < kWsMM * kWsPM; e += 128) {
+      const int co = e / kWsPM, ci2 = e % kWsPM;
+      ws_put_digits(&D->mt[0][co][ci2], kWsMM * kWsPM, ci2 < kWsMM ? Msh[ci2][co] : 0.0, sc[co]);
+    }
+    return;
+  }
   for (int e = t; e < kWsLen * kWsK; e += 128) {
     const int c = e % kWsLen, m = e / kWsLen;
     Vs[c][m] = (c < len && m < k) ? op.V[c + (size_t)m * op.ldv] : 0.0;
@@ -544,9 +569,9 @@ __global__ void __launch_bounds__(kWsThreads, kOne ? 3 : 2)
       if (rl < nrows) S.win[rr][sl] = ws_to_fixed(__longlong_as_double(S.win[rr][sl]), S.escale[rr]);
     }
     __syncwarp();
-    if (flops) {  // algorithmic work: 4 len k FP64-equivalent flops per active row
+    if (flops) {  // algorithmic work (4 len k, or 2 len^2 for a dense op) FP64-equivalent flops per active row
       const int act = __popc(__ballot_sync(0xffffffffu, tq == 0 && on0)) + __popc(__ballot_sync(0xffffffffu, tq == 0 && on1));
-      if (lane == 0) atomicAdd(flops, (unsigned long long)act * 4ull * (unsigned long long)len * (unsigned long long)k);
+      if (lane == 0) atomicAdd(flops, (unsigned long long)act * op_row_flops(op));
     }
     // Only the entries an op modifies are written back: rows of a resident window that an op
     // does not touch may be updated concurrently by other kernels on other streams (the next

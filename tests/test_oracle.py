@@ -94,3 +94,26 @@ def test_oracle_phase_times(oracle):
     t1 = oracle.ab2rht_simple(A, B, Q, Z, 8, 4, time_components=True)
     t2 = oracle.rht2ht_householder(A, B, Q, Z, 8, 4, time_components=True)
     assert all(t >= 0 for t in t1 + t2) and sum(t1) > 0 and sum(t2) > 0
+
+
+GIVENS_CASES = [(5, 2, 2, 2), (17, 3, 3, 2), (33, 4, 2, 3), (100, 16, 8, 8), (150, 8, 4, 8), (200, 16, 2, 16)]
+
+
+@pytest.mark.parametrize("n,r,p,nq", GIVENS_CASES)
+def test_oracle_givens_stage2(oracle, n, r, p, nq):
+    """The reference's Givens stage 2 (src/rht2ht.f90:696-1344), restated: backward error and
+    orthogonality within 10 n eps, exact Hessenberg zeros, and the Householder stage 2's H, T up to
+    row/column signs (both leave Q e1 = e1)."""
+    A0, B0 = make(n)
+    A1, B1, Q1, Z1 = oracle_reduce(oracle, A0, B0, r, p, nq, stage=1)
+    Ag, Bg, Qg, Zg = copies(A1, B1, Q1, Z1)
+    oracle.rht2ht_givens(Ag, Bg, Qg, Zg, r, nq)
+    tol = 10 * n * EPS
+    assert bwd(Qg, A0, Zg, Ag) <= tol and bwd(Qg, B0, Zg, Bg) <= tol
+    assert orth(Qg) <= tol and orth(Zg) <= tol
+    assert np.abs(np.tril(Ag, -2)).max(initial=0) == 0.0
+    assert np.abs(np.tril(Bg, -1)).max(initial=0) <= 100 * EPS * np.abs(Bg).max()
+    Ah, Bh, Qh, Zh = copies(A1, B1, Q1, Z1)
+    oracle.rht2ht_householder(Ah, Bh, Qh, Zh, r, nq)
+    assert abs_rel_max_diff(np.triu(Ag, -1), np.triu(Ah, -1)) < 1e-10
+    assert abs_rel_max_diff(np.triu(Bg), np.triu(Bh)) < 1e-10
