@@ -603,7 +603,7 @@ def run_pencil(args, rank: int, world: int, local: int):
     except RuntimeError:
         fp64_peak = FP64_PEAK_TFLOPS
     ms, launches = [], 0
-    kst = {"stage1": {"seconds": 0.0, "launches": 0, "flops": 0.0}, "stage2": {"seconds": 0.0, "launches": 0, "flops": 0.0}}
+    kst = {k: {"seconds": 0.0, "launches": 0, "flops": 0.0, "busy_seconds": 0.0} for k in ("stage1", "stage2")}
     fp64 = None
     check = None
     t_check = 0.0
@@ -622,7 +622,10 @@ def run_pencil(args, rank: int, world: int, local: int):
                                        "peak_source": "cuBLAS DGEMM 8192^3 measured in this run, of measured",
                                        "frac": (fst["flops"] / fst["seconds"] / 1e12 / fp64_peak
                                                 if fst["seconds"] > 0 else None),
-                                       "launches": fst["launches"], "seconds": fst["seconds"]}}
+                                       "launches": fst["launches"], "seconds": fst["seconds"],
+                                       "busy_seconds": fst["busy_seconds"],
+                                       "achieved_busy_tflops": (fst["flops"] / fst["busy_seconds"] / 1e12
+                                                                if fst["busy_seconds"] > 0 else None)}}
             if do_check:
                 tc = time.perf_counter()
                 fp64["check"] = device_check(torch, work, dev0)
@@ -686,6 +689,8 @@ def run_pencil(args, rank: int, world: int, local: int):
         pass
     s2 = kst["stage2"]
     fp64eq = s2["flops"] / s2["seconds"] / 1e12 if s2["seconds"] > 0 else None
+    # the lists run on four streams at once: flops over the time at least one of them ran
+    fp64eq_busy = s2["flops"] / s2["busy_seconds"] / 1e12 if s2["busy_seconds"] > 0 else None
     if split:
         # each FP64-equivalent flop is 43 FP16 digit-pair flops on the tensor cores (pairs t+u <= 8)
         measured = "bf16_tflops" in peaks
@@ -698,6 +703,13 @@ def run_pencil(args, rank: int, world: int, local: int):
                     "peak_source": ("MEASURED_PEAKS.json bf16_tflops (FP16 and BF16 mma run at the same rate), of measured"
                                     if measured else "1.9 PFLOP/s BF16 burst, of fallback (no MEASURED_PEAKS.json)"),
                     "fp64_equivalent_tflops": fp64eq,
+                    "aggregate": {"note": "achieved/frac divide by the mean launch duration (the contract's "
+                                          "definition); launches on the four bulk streams overlap, so this "
+                                          "divides the same flops by the time at least one launch ran",
+                                  "busy_s_per_step": s2["busy_seconds"] / max(1, steps_done),
+                                  "achieved": 43.0 * fp64eq_busy if fp64eq_busy else None,
+                                  "frac": 43.0 * fp64eq_busy / peak if fp64eq_busy else None,
+                                  "fp64_equivalent_tflops": fp64eq_busy},
                     "launches_per_step": s2["launches"] / max(1, steps_done),
                     "avg_launch_ms": 1e3 * s2["seconds"] / max(1, s2["launches"])}
     else:
@@ -706,6 +718,9 @@ def run_pencil(args, rank: int, world: int, local: int):
                     "kernel": "k_apply_left/k_apply_right<GeoS2> (FP64 compact-WY op lists)",
                     "work": "4 len k flops per strip row per op",
                     "peak_source": "cuBLAS DGEMM 8192^3 measured in this run, of measured",
+                    "aggregate": {"busy_s_per_step": s2["busy_seconds"] / max(1, steps_done),
+                                  "achieved": fp64eq_busy,
+                                  "frac": fp64eq_busy / fp64_peak if fp64eq_busy else None},
                     "launches_per_step": s2["launches"] / max(1, steps_done),
                     "avg_launch_ms": 1e3 * s2["seconds"] / max(1, s2["launches"])}
 

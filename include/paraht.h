@@ -82,8 +82,11 @@ int paraht_ctx_fill_residue(paraht_ctx ctx, double* residue, int nres);
 /* With PARAHT_FLAG_KERNEL_TIMES, for the bulk compact-WY op-list kernels of the last call (the
  * split-precision kernel under PARAHT_FLAG_SPLIT, else the FP64 kernels; the FP64 path's 8-row
  * critical-path lists are not timed): [0] summed launch durations (s), [1] launches,
- * [2] algorithmic FP64-equivalent flops (4 len k per strip row per op) of the stage-1 lists;
- * [3..5] the same for the stage-2 lists.  No counterpart in the reference. */
+ * [2] algorithmic FP64-equivalent flops (4 len k per strip row per op, 2 len^2 for the Givens
+ * stage's dense ops) of the stage-1 lists; [3..5] the same for the stage-2 lists; [6], [7] the
+ * time during which at least one stage-1 / stage-2 list ran (the union of the launch intervals:
+ * lists on different streams overlap, so their durations add up to more than the elapsed time).
+ * No counterpart in the reference. */
 int paraht_ctx_kernel_stats(paraht_ctx ctx, double* stats, int nstats);
 
 /* ---- host-pointer drop-ins (copy in, reduce on the GPU, copy out) ----

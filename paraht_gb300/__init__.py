@@ -156,10 +156,10 @@ class Context:
         """Split-precision op-list kernel statistics of the last call made with
         PARAHT_FLAG_KERNEL_TIMES: per stage, summed launch seconds, launches and algorithmic
         FP64-equivalent flops."""
-        out = (C.c_double * 6)()
-        check(lib().paraht_ctx_kernel_stats(self._h, out, 6), "kernel_stats")
-        return {"stage1": {"seconds": out[0], "launches": int(out[1]), "flops": out[2]},
-                "stage2": {"seconds": out[3], "launches": int(out[4]), "flops": out[5]}}
+        out = (C.c_double * 8)()
+        check(lib().paraht_ctx_kernel_stats(self._h, out, 8), "kernel_stats")
+        return {"stage1": {"seconds": out[0], "launches": int(out[1]), "flops": out[2], "busy_seconds": out[6]},
+                "stage2": {"seconds": out[3], "launches": int(out[4]), "flops": out[5], "busy_seconds": out[7]}}
 
     def rht2ht_d_noalloc(self, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, nq, flags=0):
         """paraht_rht2ht_d with the scratch in a fixed device array (no allocation; calls that

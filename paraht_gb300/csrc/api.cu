@@ -236,6 +236,7 @@ extern "C" int paraht_ctx_destroy(paraht_ctx c) {
   if (x.ev_a) cudaEventDestroy(x.ev_a);
   if (x.ev_b) cudaEventDestroy(x.ev_b);
   for (auto e : x.kc.ev) cudaEventDestroy(e);
+  if (x.kc.ref) cudaEventDestroy(x.kc.ref);
   if (x.kc.dflops) cudaFree(x.kc.dflops);
   for (auto e : x.ev)
     if (e) cudaEventDestroy(e);
@@ -280,7 +281,7 @@ extern "C" int paraht_ctx_launch_count(paraht_ctx c, long long* count) {
 extern "C" int paraht_ctx_kernel_stats(paraht_ctx c, double* st, int ns) {
   if (!ctx_ok(c)) return PARAHT_ERR_BAD_CTX;
   if (!st) return -2;
-  for (int i = 0; i < ns && i < 6; ++i) st[i] = c->c.kstats[i];
+  for (int i = 0; i < ns && i < 8; ++i) st[i] = c->c.kstats[i];
   return 0;
 }
 
@@ -345,6 +346,12 @@ static int run_device(Ctx& x, int which, int n, double* A, int lda, double* B, i
       return PARAHT_ERR_ALLOC;
     }
     cudaMemsetAsync(x.kc.dflops, 0, 2 * sizeof(unsigned long long), x.stream);
+    if (!x.kc.ref && cudaEventCreate(&x.kc.ref) != cudaSuccess) {
+      cudaGetLastError();
+      x.kc.ref = nullptr;
+      return PARAHT_ERR_CUDA;
+    }
+    cudaEventRecord(x.kc.ref, x.stream);
     x.kc.used = 0;
     pht::tl_kclock = &x.kc;
   }
@@ -397,14 +404,36 @@ static int run_device(Ctx& x, int which, int n, double* A, int lda, double* B, i
   if (!rc && hstatus) rc = hstatus;
   pht::tl_kclock = nullptr;
   if (!rc && ktimes) {  // all streams have joined the main stream, which finish() synchronized
+    // per launch: duration, and its interval relative to the reference event; the union of the
+    // intervals of a site is the time during which at least one of its launches ran (launches on
+    // different streams overlap)
+    std::vector<std::pair<float, float>> iv[2];
     for (size_t i = 0; i < x.kc.used; ++i) {
-      float ms = 0.f;
-      if (cudaEventElapsedTime(&ms, x.kc.ev[2 * i], x.kc.ev[2 * i + 1]) != cudaSuccess) {
+      float ms = 0.f, a = 0.f, b = 0.f;
+      if (cudaEventElapsedTime(&ms, x.kc.ev[2 * i], x.kc.ev[2 * i + 1]) != cudaSuccess ||
+          cudaEventElapsedTime(&a, x.kc.ref, x.kc.ev[2 * i]) != cudaSuccess ||
+          cudaEventElapsedTime(&b, x.kc.ref, x.kc.ev[2 * i + 1]) != cudaSuccess) {
         cudaGetLastError();
         continue;
       }
       x.kstats[3 * x.kc.site[i]] += ms * 1e-3;
       x.kstats[3 * x.kc.site[i] + 1] += 1.0;
+      iv[x.kc.site[i] & 1].push_back({a, b});
+    }
+    for (int st = 0; st < 2; ++st) {
+      std::sort(iv[st].begin(), iv[st].end());
+      double busy = 0.0, lo = 0.0, hi = -1.0;
+      for (const auto& p : iv[st]) {
+        if (p.first > hi) {
+          if (hi > lo) busy += hi - lo;
+          lo = p.first;
+          hi = p.second;
+        } else if (p.second > hi) {
+          hi = p.second;
+        }
+      }
+      if (hi > lo) busy += hi - lo;
+      x.kstats[6 + st] = busy * 1e-3;
     }
     unsigned long long fl[2] = {0, 0};
     cudaMemcpy(fl, x.kc.dflops, sizeof(fl), cudaMemcpyDeviceToHost);

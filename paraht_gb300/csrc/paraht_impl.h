@@ -85,8 +85,9 @@ struct Ctx {
     std::vector<cudaEvent_t> ev;
     std::vector<int> site;
     size_t used = 0;
+    cudaEvent_t ref = nullptr;  // recorded on the context's stream before the call's first launch
   } kc;
-  double kstats[6] = {0};
+  double kstats[8] = {0};
   // persistent batched kernel (batched.cu): its device buffer (pencil table, queue counter,
   // per-CTA workspace), the host image of the table, and the stream it runs on while the
   // pencils it does not take go through the single-pencil path

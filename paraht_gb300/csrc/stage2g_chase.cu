@@ -37,6 +37,8 @@
 namespace pht {
 
 constexpr int kGChaseThreads = 256;
+// R: the largest band the instantiation takes (16 or 32; a block column fits one warp, and a row
+// of a block is held in R registers)
 
 struct GChaseArgs {
   double* A;
@@ -121,7 +123,73 @@ static __device__ void g_delayed_left(const S2GStore& S, int ib, int m, double* 
   __syncthreads();
 }
 
+// G <- G * (the step's rotations ig = nb-1 .. 1) for the ldu rows of G, one lane per row: the
+// left rotations as drot(U(:, ic-1+ig), U(:, ic+ig)) (:975-980), the right ones as
+// drot(V(:, ic+ig), V(:, ic+ig-1)) (:990-995).  The step touches columns ic-1 .. ic+nb-2
+// (0-based), held in registers (w[j] = column ic-1+j).
+template <int R, bool kLeft>
+static __device__ __noinline__ void g_accumulate(double* G, int ldu, int ic, int nb, const double* cs,
+                                                 const double* sns, int lane) {
+  for (int row = lane; row < ldu; row += 32) {
+    double* Gr = G + row + (size_t)(ic - 1) * ldu;
+    double w[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) w[j] = j < nb ? Gr[(size_t)j * ldu] : 0.0;
+    double carry = w[R - 1];
+#pragma unroll
+    for (int ig = R - 1; ig >= 1; --ig) {
+      if (ig > nb - 1) {
+        carry = w[ig - 1];
+        continue;
+      }
+      const double c = cs[ig], sn = sns[ig];
+      const double v = w[ig - 1];
+      if (kLeft) {  // x = column ic-2+ig, y = ic-1+ig
+        w[ig] = fma(c, carry, -sn * v);
+        carry = fma(c, v, sn * carry);
+      } else {  // x = column ic-1+ig, y = ic-2+ig
+        w[ig] = fma(c, carry, sn * v);
+        carry = fma(c, v, -sn * carry);
+      }
+    }
+    w[0] = carry;
+#pragma unroll
+    for (int j = 0; j < R; ++j)
+      if (j < nb) Gr[(size_t)j * ldu] = w[j];
+  }
+}
+
+// Right rotations of the step (cv, sv) on `rows` rows of X starting at `row0` (one row per thread
+// t0 + k * stride), columns p0 .. p0+nb-1 held in R registers per row.
+template <int R>
+static __device__ __noinline__ void g_rows_right(double* X, int ld, int row0, int rows, int p0, int nb, const double* cv,
+                                                 const double* sv, int t0, int stride) {
+  for (int e = t0; e < rows; e += stride) {
+    double* row = X + (size_t)(row0 + e - 1) + (size_t)(p0 - 1) * ld;
+    double v[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) v[j] = j < nb ? row[(size_t)j * ld] : 0.0;
+    double carry = v[R - 1];
+#pragma unroll
+    for (int ig = R - 1; ig >= 1; --ig) {
+      if (ig > nb - 1) {
+        carry = v[ig - 1];
+        continue;
+      }
+      const double c = cv[ig], sn = sv[ig];
+      const double yv = v[ig - 1];
+      v[ig] = fma(c, carry, sn * yv);
+      carry = fma(c, yv, -sn * carry);
+    }
+    v[0] = carry;
+#pragma unroll
+    for (int j = 0; j < R; ++j)
+      if (j < nb) row[(size_t)j * ld] = v[j];
+  }
+}
+
 // One sweep: src/rht2ht.f90:788-957 for column jc = J + ic - 1.
+template <int R>
 static __device__ void g_run_sweep(const GChaseArgs& a, int ic, GSm& s) {
   double* A = a.A;
   double* B = a.B;
@@ -238,51 +306,22 @@ static __device__ void g_run_sweep(const GChaseArgs& a, int ic, GSm& s) {
     {
       const int nA = min(n, p0 + r + nb - 1) - p0 + 1, nAbove = p0 - istart;
       const int total = nA + 2 * nAbove;
-      for (int e = t; e < total; e += nt) {
-        double* row;
-        int ld;
-        if (e < nA) {
-          row = &A1(p0 + e, p0);
-          ld = lda;
-        } else if (e < nA + nAbove) {
-          row = &A1(istart + e - nA, p0);
-          ld = lda;
-        } else {
-          row = &B1(istart + e - nA - nAbove, p0);
-          ld = ldb;
-        }
-        double carry = row[(size_t)(nb - 1) * ld];
-        for (int ig = nb - 1; ig >= 1; --ig) {
-          const double c = s.cv[ig], sn = s.sv[ig];
-          const double yv = row[(size_t)(ig - 1) * ld];
-          row[(size_t)ig * ld] = fma(c, carry, sn * yv);
-          carry = fma(c, yv, -sn * carry);
-        }
-        row[0] = carry;
+      // one flat index over the three row ranges, so that every thread has a row
+      for (int e0 = 0; e0 < total; e0 += nt) {
+        const int e = e0 + t;
+        if (e < nA)
+          g_rows_right<R>(A, lda, p0 + e, 1, p0, nb, s.cv, s.sv, 0, 1);
+        else if (e < nA + nAbove)
+          g_rows_right<R>(A, lda, istart + e - nA, 1, p0, nb, s.cv, s.sv, 0, 1);
+        else if (e < total)
+          g_rows_right<R>(B, ldb, istart + e - nA - nAbove, 1, p0, nb, s.cv, s.sv, 0, 1);
       }
     }
     // 6. the step's rotations into U(ib), V(ib) (:970-1003), the right ones kept as (c, s)
-    if (t < 64) {
-      const bool left = t < 32;
-      double* G = (left ? S.U : S.V) + S.gi(1, 1, ib);
-      const double* cs = left ? s.cu : s.cv;
-      const double* sns = left ? s.su : s.sv;
-      for (int row = lane; row < ldu; row += 32) {
-        double* Gr = G + row;
-        double carry = Gr[(size_t)(ic + nb - 2) * ldu];
-        for (int ig = nb - 1; ig >= 1; --ig) {
-          const double c = cs[ig], sn = sns[ig];
-          const double v = Gr[(size_t)(ic - 2 + ig) * ldu];
-          if (left) {  // drot(U(:, ic-1+ig), U(:, ic+ig)): x = column ic-2+ig (0-based), y = ic-1+ig
-            Gr[(size_t)(ic - 1 + ig) * ldu] = fma(c, carry, -sn * v);
-            carry = fma(c, v, sn * carry);
-          } else {  // drot(V(:, ic+ig), V(:, ic+ig-1)): x = column ic-1+ig (0-based), y = ic-2+ig
-            Gr[(size_t)(ic - 1 + ig) * ldu] = fma(c, carry, sn * v);
-            carry = fma(c, v, -sn * carry);
-          }
-        }
-        Gr[(size_t)(ic - 1) * ldu] = carry;
-      }
+    if (t < 32) {
+      g_accumulate<R, true>(S.U + S.gi(1, 1, ib), ldu, ic, nb, s.cu, s.su, lane);
+    } else if (t < 64) {
+      g_accumulate<R, false>(S.V + S.gi(1, 1, ib), ldu, ic, nb, s.cv, s.sv, lane);
     } else if (t < 64 + 32) {
       for (int ig = t - 64 + 1; ig <= nb - 1; ig += 32) {
         S.CV[S.ri(ic + ig - 1, ic, ib)] = s.cv[ig];
@@ -296,6 +335,7 @@ static __device__ void g_run_sweep(const GChaseArgs& a, int ic, GSm& s) {
 #undef B1
 }
 
+template <int R>
 __global__ void __launch_bounds__(kGChaseThreads, 1) k_s2g_chase(GChaseArgs a) {
   extern __shared__ double gsm[];
   __shared__ int s_ic, s_abort;
@@ -311,12 +351,12 @@ __global__ void __launch_bounds__(kGChaseThreads, 1) k_s2g_chase(GChaseArgs a) {
   if (threadIdx.x == 0) s_abort = 0;
   if (!a.pipelined) {
     __syncthreads();
-    for (int ic = 1; ic <= a.nq; ++ic) g_run_sweep(a, ic, s);
+    for (int ic = 1; ic <= a.nq; ++ic) g_run_sweep<R>(a, ic, s);
     return;
   }
   if (threadIdx.x == 0) s_ic = atomicAdd(a.sync.ticket, 1) + 1;
   __syncthreads();
-  g_run_sweep(a, s_ic, s);
+  g_run_sweep<R>(a, s_ic, s);
 }
 
 void s2g_launch_chase(cudaStream_t st, double* A, int lda, double* B, int ldb, int n, int J, int r, int nq,
@@ -339,7 +379,10 @@ void s2g_launch_chase(cudaStream_t st, double* A, int lda, double* B, int ldb, i
     cudaMemsetAsync(sync.ticket, 0, sizeof(int), st);
   }
   count_launch();
-  k_s2g_chase<<<a.pipelined ? nq : 1, kGChaseThreads, g_chase_smem_bytes(r, nq), st>>>(a);
+  if (r <= 16)
+    k_s2g_chase<16><<<a.pipelined ? nq : 1, kGChaseThreads, g_chase_smem_bytes(r, nq), st>>>(a);
+  else
+    k_s2g_chase<32><<<a.pipelined ? nq : 1, kGChaseThreads, g_chase_smem_bytes(r, nq), st>>>(a);
 }
 
 }  // namespace pht

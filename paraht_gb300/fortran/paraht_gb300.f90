@@ -1,8 +1,9 @@
 ! paraht_gb300.f90 -- Fortran drop-in for the reduction path, calling libparaht (include/paraht.h)
 ! through ISO_C_BINDING.
 !
-! The modules `ab2rht` and `rht2ht` export `ab2rht_simple` and `rht2ht_householder` with exactly
-! the argument lists of the reference (src/ab2rht.f90:8-13, src/rht2ht.f90:1346-1351), so a
+! The modules `ab2rht` and `rht2ht` export `ab2rht_simple`, `rht2ht_householder` and
+! `rht2ht_givens` with exactly the argument lists of the reference (src/ab2rht.f90:8-13,
+! src/rht2ht.f90:1346-1351, src/rht2ht.f90:696-700), so a
 ! caller such as src/profilereduction.f90 only needs to be recompiled against this file and
 ! linked with -lparaht.  Arrays stay on the host; each call copies them to the GPU, reduces and
 ! copies them back.  An optional trailing INFO argument returns the library status (0 = ok,
@@ -30,6 +31,13 @@ module paraht_c
          integer(c_int), value :: n, lda, ldb, ldq, ldz, r, nq, time_components
          real(c_double) :: A(*), B(*), Q(*), Z(*)
       end function paraht_rht2ht
+
+      integer(c_int) function paraht_rht2ht_givens(n, A, lda, B, ldb, Q, ldq, Z, ldz, r, nq) &
+         bind(C, name="paraht_rht2ht_givens")
+         import :: c_int, c_double
+         integer(c_int), value :: n, lda, ldb, ldq, ldz, r, nq
+         real(c_double) :: A(*), B(*), Q(*), Z(*)
+      end function paraht_rht2ht_givens
 
       integer(c_int) function paraht_reduce(n, A, lda, B, ldb, Q, ldq, Z, ldz, r, p, nq, flags) &
          bind(C, name="paraht_reduce")
@@ -99,4 +107,15 @@ contains
          Z, int(ldz, c_int), int(r, c_int), int(nq, c_int), tc)
       call paraht_report('rht2ht_householder', status, info)
    end subroutine rht2ht_householder
+
+   ! src/rht2ht.f90:696 -- stage 2 with Givens rotations (r <= 32, r + nq <= 64 on the GPU)
+   subroutine rht2ht_givens(n, A, lda, B, ldb, Q, ldq, Z, ldz, r, nq, info)
+      integer, intent(in) :: n, lda, ldb, ldq, ldz, r, nq
+      double precision, intent(inout) :: A(lda,*), B(ldb,*), Z(ldz,*), Q(ldq,*)
+      integer, intent(out), optional :: info
+      integer(c_int) :: status
+      status = paraht_rht2ht_givens(int(n, c_int), A, int(lda, c_int), B, int(ldb, c_int), Q, int(ldq, c_int), &
+         Z, int(ldz, c_int), int(r, c_int), int(nq, c_int))
+      call paraht_report('rht2ht_givens', status, info)
+   end subroutine rht2ht_givens
 end module rht2ht
