@@ -19,8 +19,9 @@ and the CPU baselines.  ``steps`` is the number of split reductions actually tim
 ``steps_requested`` the --steps asked for.
 
 * ``value``: mean device time per split step (CUDA events on the library's stream, max over ranks).
-* ``fp64``: the all-FP64 path's device time for one reduction at its tuned (r, p, nq), its
-  backward errors, and ``split_vs_fp64`` = fp64 seconds / split seconds.
+* ``fp64``: the all-FP64 path's device time for one reduction at its tuned (r, p, nq) and stage-2
+  variant (small reflectors), its backward errors, and ``split_vs_fp64`` = fp64 seconds / split
+  seconds.  The split path runs its faster stage-2 variant, Givens rotations (--stage2).
 * ``check``: backward errors ||Q^T A0 Z - H||/||A0||, ||Q^T B0 Z - T||/||B0|| and orthogonality
   ||Q^T Q - I||_F, ||Z^T Z - I||_F of the last split step (FP64 GEMMs on the device).
 * ``e2e``: one split reduction through the public host entry point paraht_reduce_host with
@@ -96,8 +97,11 @@ def parse(argv=None):
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison step")
     ap.add_argument("--dist", default="std")
     ap.add_argument("--precision", choices=("fp64", "split"), default="split")
-    ap.add_argument("--stage2", choices=("householder", "givens"), default="householder",
-                    help="stage-2 variant: small reflectors (rht2ht_householder) or Givens rotations (rht2ht_givens)")
+    ap.add_argument("--stage2", choices=("householder", "givens"), default="givens",
+                    help="stage-2 variant of the timed path: Givens rotations (rht2ht_givens, the faster split "
+                         "path) or small reflectors (rht2ht_householder)")
+    ap.add_argument("--fp64-stage2", choices=("householder", "givens"), default="householder",
+                    help="stage-2 variant of the FP64 comparison step (small reflectors: the faster FP64 path)")
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--cpu-sample-n", type=int, default=4000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -521,6 +525,7 @@ def run_pencil(args, rank: int, world: int, local: int):
     n, r, p, nq = args.n, args.r, args.p, args.nq
     split = args.precision == "split"
     variant = ph.PARAHT_FLAG_GIVENS if args.stage2 == "givens" else 0
+    fvariant = ph.PARAHT_FLAG_GIVENS if args.fp64_stage2 == "givens" else 0
     flags = (ph.PARAHT_FLAG_SPLIT if split else 0) | variant
     fr, fp, fnq = (int(x) for x in args.fp64_params.split(","))
     do_fp64 = split and not args.no_fp64
@@ -582,14 +587,14 @@ def run_pencil(args, rank: int, world: int, local: int):
     sdev = [torch.from_numpy(np.ascontiguousarray(X.T)).cuda() for X in small0]
     seye = torch.eye(nw, dtype=torch.float64, device="cuda")
     swork = [torch.empty_like(seye) for _ in range(4)]
-    warm_sets = [((r, p, nq), flags)] + ([((fr, fp, fnq), variant)] if do_fp64 else [])
+    warm_sets = [((r, p, nq), flags)] + ([((fr, fp, fnq), fvariant)] if do_fp64 else [])
     for i in range(max(0, args.warmup - 1)):
         prm, f = warm_sets[i % len(warm_sets)]
         restore(swork, (sdev[0], sdev[1], seye, seye))
         launch(swork, nw, prm, f)
     if do_fp64 and args.warmup < 3:  # the FP64 parameter set gets at least one small warm-up
         restore(swork, (sdev[0], sdev[1], seye, seye))
-        launch(swork, nw, (fr, fp, fnq), variant)
+        launch(swork, nw, (fr, fp, fnq), fvariant)
     del swork, sdev, seye
     t0w = time.perf_counter()
     if args.warmup > 0:
@@ -611,10 +616,10 @@ def run_pencil(args, rank: int, world: int, local: int):
     with sampler:
         # ---- one FP64 reduction at the FP64 path's own parameters ----
         if do_fp64:
-            t_f = timed((fr, fp, fnq), variant | ph.PARAHT_FLAG_KERNEL_TIMES)
+            t_f = timed((fr, fp, fnq), fvariant | ph.PARAHT_FLAG_KERNEL_TIMES)
             t_f = job_time(t_f, "cuda")
             fst = ctx.kernel_stats()["stage2"]
-            fp64 = {"seconds": t_f, "r": fr, "p": fp, "nq": fnq, "launches": ctx.launch_count(),
+            fp64 = {"seconds": t_f, "r": fr, "p": fp, "nq": fnq, "stage2": args.fp64_stage2, "launches": ctx.launch_count(),
                     "effective_gflops": flops_nominal(n) / t_f / 1e9,
                     "op_list_kernel": {"kernel": "k_apply_left/k_apply_right<GeoS2> (FP64 compact-WY op lists)",
                                        "achieved_tflops": fst["flops"] / fst["seconds"] / 1e12 if fst["seconds"] > 0 else None,

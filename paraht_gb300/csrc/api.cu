@@ -183,6 +183,14 @@ extern "C" int paraht_ctx_create(paraht_ctx* out, int device) {
   if (!rc && cudaEventCreateWithFlags(&x.ev_a, cudaEventDisableTiming) != cudaSuccess) rc = PARAHT_ERR_CUDA;
   if (!rc && cudaEventCreateWithFlags(&x.ev_b, cudaEventDisableTiming) != cudaSuccess) rc = PARAHT_ERR_CUDA;
   if (!rc && cudaStreamCreateWithFlags(&x.side2, cudaStreamNonBlocking) != cudaSuccess) rc = PARAHT_ERR_CUDA;
+  {
+    int least = 0, greatest = 0;
+    if (!rc && cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) rc = PARAHT_ERR_CUDA;
+    if (!rc && cudaStreamCreateWithPriority(&x.crit, cudaStreamNonBlocking, greatest) != cudaSuccess)
+      rc = PARAHT_ERR_CUDA;
+    if (!rc && cudaEventCreateWithFlags(&x.ev_enter, cudaEventDisableTiming) != cudaSuccess) rc = PARAHT_ERR_CUDA;
+    if (!rc && cudaEventCreateWithFlags(&x.ev_exit, cudaEventDisableTiming) != cudaSuccess) rc = PARAHT_ERR_CUDA;
+  }
   if (!rc && cudaStreamCreateWithFlags(&x.side3, cudaStreamNonBlocking) != cudaSuccess) rc = PARAHT_ERR_CUDA;
   if (!rc && cudaStreamCreateWithFlags(&x.side4, cudaStreamNonBlocking) != cudaSuccess) rc = PARAHT_ERR_CUDA;
   for (auto& e : x.ev_s2)
@@ -218,13 +226,15 @@ extern "C" int paraht_ctx_destroy(paraht_ctx c) {
     cudaStreamSynchronize(x.side);
     cudaStreamDestroy(x.side);
   }
-  for (cudaStream_t* sp : {&x.side2, &x.side3, &x.side4})
+  for (cudaStream_t* sp : {&x.side2, &x.side3, &x.side4, &x.crit})
     if (*sp) {
       cudaStreamSynchronize(*sp);
       cudaStreamDestroy(*sp);
     }
   for (auto e : x.ev_s2)
     if (e) cudaEventDestroy(e);
+  if (x.ev_enter) cudaEventDestroy(x.ev_enter);
+  if (x.ev_exit) cudaEventDestroy(x.ev_exit);
   if (x.bstream) {
     cudaStreamSynchronize(x.bstream);
     cudaStreamDestroy(x.bstream);
@@ -326,8 +336,26 @@ static int finish(Ctx& x) {
 }
 
 // Runs the selected stages on device-resident arrays (stream-ordered; caller synchronises).
+static int run_device_on(Ctx& x, int which, int n, double* A, int lda, double* B, int ldb, double* Q, int ldq,
+                         double* Z, int ldz, int r, int p, int nq, int flags);
+// The same on the context's high-priority stream, which waits for the work already queued on the
+// caller's stream and which the caller's stream then waits for.
 static int run_device(Ctx& x, int which, int n, double* A, int lda, double* B, int ldb, double* Q, int ldq, double* Z,
                       int ldz, int r, int p, int nq, int flags) {
+  if (!x.crit || n == 0) return run_device_on(x, which, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, p, nq, flags);
+  cudaStream_t user = x.stream;
+  cudaEventRecord(x.ev_enter, user);
+  cudaStreamWaitEvent(x.crit, x.ev_enter, 0);
+  x.stream = x.crit;
+  const int rc = run_device_on(x, which, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, p, nq, flags);
+  x.stream = user;
+  cudaEventRecord(x.ev_exit, x.crit);
+  cudaStreamWaitEvent(user, x.ev_exit, 0);
+  return rc;
+}
+
+static int run_device_on(Ctx& x, int which, int n, double* A, int lda, double* B, int ldb, double* Q, int ldq,
+                         double* Z, int ldz, int r, int p, int nq, int flags) {
   x.launches = 0;
   if (n == 0) return 0;
   x.split = (flags & PARAHT_FLAG_SPLIT) ? 1 : 0;

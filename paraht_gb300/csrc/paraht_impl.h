@@ -60,6 +60,12 @@ struct Ctx {
   cudaStream_t side = nullptr;      // second stream for work that overlaps the critical path
   cudaStream_t side2 = nullptr;     // third stream (bulk updates that feed nothing on the critical path)
   cudaStream_t side3 = nullptr, side4 = nullptr;  // stage-2 bulk updates of Q and Z beside those of A, B
+  // highest-priority stream for the critical path (generation chains, chase, lookahead): the bulk
+  // op-list CTAs live for a whole list and fill the SMs, so a chain kernel waits for a free CTA
+  // slot, and the scheduler gives freed slots to the highest-priority stream first.  Calls run on
+  // it, joined to the caller's stream by ev_enter / ev_exit.
+  cudaStream_t crit = nullptr;
+  cudaEvent_t ev_enter = nullptr, ev_exit = nullptr;
   cudaEvent_t ev_a = nullptr, ev_b = nullptr;
   cudaEvent_t ev_s2[4] = {};        // stage-2 bulk chains: operands prepared, and the joins of A, Q, Z
   cudaEvent_t ev[8] = {};           // stage-1 dependency events
