@@ -247,7 +247,7 @@ static __device__ void s1_rgen_body(const double* __restrict__ B, int ldb, const
   double* tauL = tauR + L;              // nb
   double* G2 = tauL + nb;               // nb*nb
   double* Ts = G2 + nb * nb;            // nb*nb
-  double* sc = Ts + nb * nb;            // 4, then 4 (L+1) for the published RQ reflectors
+  double* sc = Ts + nb * nb;            // 4, then 2 (L+1) for the published RQ reflectors
   const int t = threadIdx.x;
   for (int e = t; e < nb2 * nb2; e += blockDim.x) {
     const int i = e % nb2, j = e / nb2;
@@ -255,47 +255,27 @@ static __device__ void s1_rgen_body(const double* __restrict__ B, int ldb, const
   }
   __syncthreads();
   // ---- RQ (dgerq2): rows bottom to top; the reflector of row i acts on columns 0..i ----
-  // Warp 0 forms the reflectors (the critical chain): in round s it applies reflector s to row
-  // s-1 and forms reflector s-1 from it.  Warps 1.. own the remaining rows, each row always by the
-  // same 4-lane group, so every row receives the reflectors in order from one owner.  In round s
-  // the owner warp of row s-2 (the row warp 0 needs next) first applies reflector s to it with all
-  // 32 lanes and only then arrives on early(s); the other warps arrive at once; then every warp
-  // updates its remaining rows.  Warp 0 waits only for early(s+1) before round s, so its chain
-  // overlaps the bulk of the row updates instead of alternating with it.  Reflectors go through
-  // kRqSlots slots: warp 0 writes reflector r into slot r % kRqSlots after early(r+2), when every
-  // other thread has finished round r+3 and so no longer reads the slot's previous reflector r+4.
-  // Named barriers: ready(s) = 1 + s % 4 (warp 0 arrives after publishing reflector s, the others
-  // wait), early(s) = 5 + s % 2 (the others arrive, warp 0 waits), for s = nb2-1 .. 1 and
-  // s = nb2-1 .. 2 respectively; each id has at most one generation in flight (a ready id is
-  // reused four rounds later, after warp 0 waited for early() of a round after it).
+  // Warp 0 forms the reflectors: in round s it applies reflector s to row s-1 and forms reflector
+  // s-1 from it (the critical chain); warps 1.. apply reflector s to the rows below s-1 in the
+  // same round (FP64 throughput), so the two overlap.  They hand over through named barriers:
+  // ready[s&1] (reflector s published; warp 0 arrives, the others wait) and done[s&1] (rows below
+  // s-1 updated by reflector s; the others arrive, warp 0 waits before it touches row s-2).
+  // Same-parity generations never overlap: warp 0 publishes reflector r only after waiting for
+  // done(r+2), which the others signal after consuming ready(r+2); the others signal done(s) only
+  // after waiting for ready(s), which warp 0 publishes after consuming done(s+2).
   {
-    constexpr int kRqSlots = 4;
     const int nthr = blockDim.x, lane = t & 31;
-    double* pv = sc + 4;  // kRqSlots published reflectors: v[0..L-1] (v_s = 1 implied), tau at [L]
+    double* pv = sc + 4;  // two published reflectors: v[0..L-1] (v_s = 1 implied), tau at [L]
     auto bar_sync = [&](int id) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthr) : "memory"); };
     auto bar_arrive = [&](int id) { asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(nthr) : "memory"); };
-    auto ready_id = [](int sr) { return 1 + (sr & 3); };
-    auto early_id = [](int sr) { return 5 + (sr & 1); };
-    // x <- x H(s) for row x of S with one warp (32 lanes): reflector s = slot v, tau v[L]
-    auto apply_row_warp = [&](int x, int sr, const double* v) {
-      const double tau = v[L];
-      double d = 0.0;
-      for (int c = lane; c < sr; c += 32) d = fma(S[x + c * lds], v[c], d);
-      d = warp_sum(d);
-      if (tau != 0.0) {
-        const double tw = tau * (S[x + sr * lds] + d);
-        for (int c = lane; c < sr; c += 32) S[x + c * lds] = fma(-tw, v[c], S[x + c * lds]);
-        if (lane == 0) S[x + sr * lds] -= tw;
-      }
-    };
     if (t < 32) {
-      // reflector of row r from its current values: scaled tail into S and slot r % kRqSlots
+      // reflector of row r from its current values: scaled tail into S and the publish slot
       auto form = [&](int r) {
         double sg = 0.0;
         for (int c = lane; c < r; c += 32) sg = fma(S[r + c * lds], S[r + c * lds], sg);
         sg = warp_sum(sg);
         const Reflector h = reflector_from_norm2(S[r + r * lds], sg);
-        double* v = pv + (r % kRqSlots) * (L + 1);
+        double* v = pv + (r & 1) * (L + 1);
         for (int c = lane; c < r; c += 32) {
           const double x = S[r + c * lds] * h.scal;
           S[r + c * lds] = x;
@@ -310,37 +290,39 @@ static __device__ void s1_rgen_body(const double* __restrict__ B, int ldb, const
       if (nb2 >= 1) form(nb2 - 1);
       if (nb2 - 1 >= 1) {
         __threadfence_block();
-        bar_arrive(ready_id(nb2 - 1));
+        bar_arrive(1 + ((nb2 - 1) & 1));
       }
       for (int sr = nb2 - 1; sr >= 1; --sr) {
-        if (sr + 1 <= nb2 - 1) bar_sync(early_id(sr + 1));  // row sr-1 has every reflector > sr
+        if (sr <= nb2 - 2) bar_sync(3 + ((sr + 1) & 1));
+        const double* v = pv + (sr & 1) * (L + 1);
+        const double tau = v[L];
         const int r = sr - 1;
-        apply_row_warp(r, sr, pv + (sr % kRqSlots) * (L + 1));
+        double d = 0.0;
+        for (int c = lane; c < sr; c += 32) d = fma(S[r + c * lds], v[c], d);
+        d = warp_sum(d);
+        if (tau != 0.0) {
+          const double tw = tau * (S[r + sr * lds] + d);
+          for (int c = lane; c < sr; c += 32) S[r + c * lds] = fma(-tw, v[c], S[r + c * lds]);
+          if (lane == 0) S[r + sr * lds] -= tw;
+        }
         __syncwarp();
         form(r);
         if (r >= 1) {
           __threadfence_block();
-          bar_arrive(ready_id(r));
+          bar_arrive(1 + (r & 1));
         }
       }
+      if (nb2 - 1 >= 1) bar_sync(3 + (1 & 1));  // done(1)
     } else {
       const int u = t - 32, g = u / Q, qq = u % Q, G = (nthr - 32) / Q;
-      const int wme = t >> 5;  // this warp (1 ..)
       for (int sr = nb2 - 1; sr >= 1; --sr) {
-        bar_sync(ready_id(sr));
-        const double* v = pv + (sr % kRqSlots) * (L + 1);
+        bar_sync(1 + (sr & 1));
+        const double* v = pv + (sr & 1) * (L + 1);
         const double tau = v[L];
-        const int early = sr - 2;  // the row warp 0 needs next; owner warp of row x: 1 + (x % G) / 8
-        if (early >= 0 && wme == 1 + (early % G) / 8) {
-          apply_row_warp(early, sr, v);
-          __threadfence_block();
-        }
-        if (early >= 0) bar_arrive(early_id(sr));
         for (int k0 = 0; k0 * G < sr - 1; ++k0) {  // uniform over the warps of this group
           const int rr = g + G * k0;
-          const bool mine = rr < sr - 1 && rr != early;
           double a0 = 0.0, a1 = 0.0;
-          if (mine) {
+          if (rr < sr - 1) {
             int cc = qq;
             for (; cc + Q < sr; cc += 2 * Q) {
               a0 = fma(S[rr + cc * lds], v[cc], a0);
@@ -349,12 +331,14 @@ static __device__ void s1_rgen_body(const double* __restrict__ B, int ldb, const
             if (cc < sr) a0 = fma(S[rr + cc * lds], v[cc], a0);
           }
           const double dd = group_sum<Q>(a0 + a1);
-          if (mine && tau != 0.0) {
+          if (rr < sr - 1 && tau != 0.0) {
             const double tw = tau * (S[rr + sr * lds] + dd);
             for (int cc = qq; cc < sr; cc += Q) S[rr + cc * lds] = fma(-tw, v[cc], S[rr + cc * lds]);
             if (qq == 0) S[rr + sr * lds] -= tw;
           }
         }
+        __threadfence_block();
+        bar_arrive(3 + (sr & 1));
       }
     }
   }
@@ -507,7 +491,7 @@ inline size_t s1_lgen_smem(int L, int nb) {
 inline size_t s1_rgen_smem_vr(int L, int nb, bool vr) {
   const size_t p = (size_t)s1_rgen_pitch(L);
   return sizeof(double) *
-         (p * L + (size_t)nb * p + (vr ? (size_t)L * L : 0) + 2 * (size_t)L + nb + 2 * nb * nb + 4 + 4 * ((size_t)L + 1));
+         (p * L + (size_t)nb * p + (vr ? (size_t)L * L : 0) + 2 * (size_t)L + nb + 2 * nb * nb + 4 + 2 * ((size_t)L + 1));
 }
 // 4 lanes per row, a multiple of 32, and at least two warps (warp 0 forms the RQ reflectors, the
 // others update the remaining rows)
