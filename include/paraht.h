@@ -163,6 +163,27 @@ int paraht_reduce_batched_d(paraht_ctx ctx, int count, const int* n, double* con
                             double* const* B, const int* ldb, double* const* Q, const int* ldq, double* const* Z,
                             const int* ldz, const int* r, const int* p, const int* nq, int flags);
 
+/* ---- batch plans: the persistent batched launch as a replayable CUDA graph.  No counterpart in
+ * the reference.  For a fixed set of pencils (device pointers, sizes and parameters as for
+ * paraht_reduce_batched_d) reduced again and again with new values in the same arrays:
+ * paraht_batch_plan_create checks them, groups them into buckets of equal (r, p, nq) (the
+ * autotuner's per-size choice; each bucket gets its own shared-memory size and workspace),
+ * uploads each bucket's pencil table once and captures the launches (per bucket: queue reset and
+ * one persistent launch, the buckets on parallel branches) into a CUDA graph.
+ * paraht_batch_plan_launch replays it on `stream` (cudaStream_t as void*, NULL: the legacy
+ * default stream) and returns at once; synchronise the stream before reading the results.
+ * Results are bitwise those of paraht_reduce_d in FP64.  Every pencil must be one the persistent
+ * kernel takes (p r <= 64, n <= PARAHT_BATCH_MAX_N) and flags must be 0, else
+ * PARAHT_ERR_NOT_SUPPORTED; -3 flags an invalid pencil, -16 a null plan pointer.  The plan holds
+ * its own device buffers until paraht_batch_plan_destroy; replays of one plan must not overlap. ---- */
+typedef struct paraht_batch_plan_s* paraht_batch_plan;
+int paraht_batch_plan_create(paraht_ctx ctx, int count, const int* n, double* const* A, const int* lda,
+                             double* const* B, const int* ldb, double* const* Q, const int* ldq, double* const* Z,
+                             const int* ldz, const int* r, const int* p, const int* nq, int flags,
+                             paraht_batch_plan* plan);
+int paraht_batch_plan_launch(paraht_batch_plan plan, void* stream);
+int paraht_batch_plan_destroy(paraht_batch_plan plan);
+
 /* ---- LAPACK DGGHD3-compatible entry (no counterpart in the reference, which ignores ilo/ihi;
  * the argument list of dgghd3 as the reference driver calls it, src/profilereduction.f90:156,
  * without the work array): reduces rows/columns ilo..ihi (1-based) of the pencil, A and B

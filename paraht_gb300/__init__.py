@@ -29,7 +29,8 @@ from ._lib import (PARAHT_BATCH_MAX_N, PARAHT_FLAG_BATCH_LOOP, PARAHT_FLAG_CHECK
                    PARAHT_FLAG_TIME_COMPONENTS, ParahtError, check, lib)
 
 __all__ = [
-    "ab2rht_simple", "rht2ht_householder", "rht2ht_givens", "reduce", "ht", "gghd3", "Context", "ParahtError",
+    "ab2rht_simple", "rht2ht_householder", "rht2ht_givens", "reduce", "ht", "gghd3", "Context", "BatchPlan",
+    "ParahtError",
     "PARAHT_FLAG_TIME_COMPONENTS", "PARAHT_FLAG_CHECK_FINITE", "PARAHT_FLAG_SPLIT", "PARAHT_FLAG_NO_ZERO_FILL",
     "PARAHT_FLAG_SEQUENTIAL", "PARAHT_FLAG_KERNEL_TIMES", "PARAHT_FLAG_BATCH_LOOP", "PARAHT_FLAG_GIVENS",
     "PARAHT_BATCH_MAX_N",
@@ -182,6 +183,11 @@ class Context:
                                             IA(*ldqs), PA(*Zs), IA(*ldzs), IA(*rs), IA(*ps), IA(*nqs), int(flags)),
               "reduce_batched_d")
 
+    def batch_plan(self, ns, As, ldas, Bs, ldbs, Qs, ldqs, Zs, ldzs, rs, ps, nqs, flags=0):
+        """A BatchPlan: the persistent batched launch for these pencils captured as a CUDA graph
+        (paraht_batch_plan_create); replay it with .launch(stream)."""
+        return BatchPlan(self, ns, As, ldas, Bs, ldbs, Qs, ldqs, Zs, ldzs, rs, ps, nqs, flags)
+
     def selftest_wait_timeout(self, spin_limit: int = 1000) -> int:
         """Runs the chase's bounded wait on a flag nothing sets; returns the reported status
         (PARAHT_ERR_TIMEOUT, -1003, when the failure path works)."""
@@ -201,3 +207,31 @@ class Context:
         buf = (C.c_double * 2)()
         check(lib().paraht_ctx_fill_residue(self._h, buf, 2), "fill_residue")
         return float(buf[0]), float(buf[1])
+
+
+class BatchPlan:
+    """A fixed set of pencils reduced by replaying a CUDA graph (paraht_batch_plan_*)."""
+
+    def __init__(self, ctx, ns, As, ldas, Bs, ldbs, Qs, ldqs, Zs, ldzs, rs, ps, nqs, flags=0):
+        cnt = len(ns)
+        IA = C.c_int * cnt
+        PA = C.c_void_p * cnt
+        self._h = C.c_void_p()
+        self._ctx = ctx  # the plan's launches use the context's device
+        check(lib().paraht_batch_plan_create(ctx.handle, cnt, IA(*ns), PA(*As), IA(*ldas), PA(*Bs), IA(*ldbs),
+                                             PA(*Qs), IA(*ldqs), PA(*Zs), IA(*ldzs), IA(*rs), IA(*ps), IA(*nqs),
+                                             int(flags), C.byref(self._h)), "paraht_batch_plan_create")
+
+    def launch(self, stream_ptr: int = 0):
+        check(lib().paraht_batch_plan_launch(self._h, C.c_void_p(stream_ptr or None)), "paraht_batch_plan_launch")
+
+    def close(self):
+        if self._h:
+            lib().paraht_batch_plan_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

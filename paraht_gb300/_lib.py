@@ -54,6 +54,11 @@ SIGNATURES = {
     "paraht_reduce_batched_d": [C.c_void_p, _i, C.POINTER(_i), C.POINTER(_d), C.POINTER(_i), C.POINTER(_d),
                                 C.POINTER(_i), C.POINTER(_d), C.POINTER(_i), C.POINTER(_d), C.POINTER(_i),
                                 C.POINTER(_i), C.POINTER(_i), C.POINTER(_i), _i],
+    "paraht_batch_plan_create": [C.c_void_p, _i, C.POINTER(_i), C.POINTER(_d), C.POINTER(_i), C.POINTER(_d),
+                                 C.POINTER(_i), C.POINTER(_d), C.POINTER(_i), C.POINTER(_d), C.POINTER(_i),
+                                 C.POINTER(_i), C.POINTER(_i), C.POINTER(_i), _i, C.POINTER(C.c_void_p)],
+    "paraht_batch_plan_launch": [C.c_void_p, C.c_void_p],
+    "paraht_batch_plan_destroy": [C.c_void_p],
     "paraht_gghd3": [C.c_char, C.c_char, _i, _i, _i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i, _i, _i],
     "paraht_gghd3_d": [C.c_void_p, C.c_char, C.c_char, _i, _i, _i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i, _i, _i],
     "paraht_selftest_wait_timeout": [C.c_void_p, C.c_longlong],

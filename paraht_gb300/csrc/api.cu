@@ -4,6 +4,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <array>
 #include <cctype>
 #include <atomic>
 #include <mutex>
@@ -664,6 +665,139 @@ extern "C" int paraht_reduce(int n, double* A, int lda, double* B, int ldb, doub
   const int rc = default_ctx(&c);
   if (rc) return rc;
   return host_entry(c, 0, 3, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, p, nq, flags);
+}
+
+// ---- batch plans: a fixed set of pencils reduced by replaying a CUDA graph ----
+struct paraht_batch_plan_s {
+  uint32_t magic;
+  int device;
+  std::vector<void*> buckets;
+  std::vector<cudaStream_t> branch;
+  std::vector<cudaEvent_t> ev;
+  cudaStream_t cap = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int count = 0;
+};
+static const uint32_t kPlanMagic = 0x50485450u;  // "PHTP"
+
+static void plan_free(paraht_batch_plan pl) {
+  if (!pl) return;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(pl->device);
+  if (pl->exec) cudaGraphExecDestroy(pl->exec);
+  if (pl->graph) cudaGraphDestroy(pl->graph);
+  for (void* b : pl->buckets) pht::batch_bucket_destroy(b);
+  for (auto st : pl->branch)
+    if (st) cudaStreamDestroy(st);
+  for (auto e : pl->ev)
+    if (e) cudaEventDestroy(e);
+  if (pl->cap) cudaStreamDestroy(pl->cap);
+  cudaSetDevice(prev);
+  pl->magic = 0;
+  delete pl;
+}
+
+extern "C" int paraht_batch_plan_create(paraht_ctx c, int count, const int* n, double* const* A, const int* lda,
+                                        double* const* B, const int* ldb, double* const* Q, const int* ldq,
+                                        double* const* Z, const int* ldz, const int* r, const int* p, const int* nq,
+                                        int flags, paraht_batch_plan* plan) {
+  if (!plan) return -16;
+  *plan = nullptr;
+  if (!ctx_ok(c)) return PARAHT_ERR_BAD_CTX;
+  if (count < 0) return -2;
+  if (count > 0 && (!n || !A || !lda || !B || !ldb || !Q || !ldq || !Z || !ldz || !r || !p || !nq)) return -3;
+  if (flags != 0) return PARAHT_ERR_NOT_SUPPORTED;
+  for (int i = 0; i < count; ++i) {
+    if (check_args(3, 0, n[i], A[i], lda[i], B[i], ldb[i], Q[i], ldq[i], Z[i], ldz[i], r[i], p[i], nq[i])) return -3;
+    if (n[i] > PARAHT_BATCH_MAX_N || !pht::batch_eligible(n[i], r[i], p[i], nq[i])) return PARAHT_ERR_NOT_SUPPORTED;
+  }
+  Ctx& x = c->c;
+  auto* pl = new (std::nothrow) paraht_batch_plan_s();
+  if (!pl) return PARAHT_ERR_ALLOC;
+  pl->magic = kPlanMagic;
+  pl->device = x.device;
+  pl->count = count;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(x.device);
+  // buckets: pencils sharing (r, p, nq), the autotuner's per-size choice; each gets the shared-memory
+  // size and workspace of its own parameters
+  std::vector<std::pair<std::array<int, 3>, std::vector<int>>> groups;
+  for (int i = 0; i < count; ++i) {
+    if (n[i] == 0) continue;
+    const std::array<int, 3> key{r[i], p[i], nq[i]};
+    auto it = std::find_if(groups.begin(), groups.end(), [&](const auto& g) { return g.first == key; });
+    if (it == groups.end()) {
+      groups.push_back({key, {}});
+      it = groups.end() - 1;
+    }
+    it->second.push_back(i);
+  }
+  int rc = 0;
+  for (const auto& g : groups) {
+    void* b = nullptr;
+    rc = pht::batch_bucket_create(x, g.second, n, A, lda, B, ldb, Q, ldq, Z, ldz, r, p, nq, &b);
+    if (rc) break;
+    pl->buckets.push_back(b);
+  }
+  // capture: fork one branch per bucket off a private stream, join, end
+  if (!rc && cudaStreamCreateWithFlags(&pl->cap, cudaStreamNonBlocking) != cudaSuccess) rc = PARAHT_ERR_CUDA;
+  const size_t nb = pl->buckets.size();
+  for (size_t i = 0; !rc && i < nb; ++i) {
+    cudaStream_t st = nullptr;
+    cudaEvent_t e = nullptr;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) rc = PARAHT_ERR_CUDA;
+    pl->branch.push_back(st);
+    if (!rc && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) rc = PARAHT_ERR_CUDA;
+    pl->ev.push_back(e);
+  }
+  cudaEvent_t fork = nullptr;
+  if (!rc && cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) != cudaSuccess) rc = PARAHT_ERR_CUDA;
+  if (fork) pl->ev.push_back(fork);
+  if (!rc && cudaStreamBeginCapture(pl->cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) rc = PARAHT_ERR_CUDA;
+  if (!rc) {
+    cudaEventRecord(fork, pl->cap);
+    const long long l0 = pht::tl_launches;
+    for (size_t i = 0; i < nb; ++i) {
+      cudaStreamWaitEvent(pl->branch[i], fork, 0);
+      pht::batch_bucket_enqueue(pl->buckets[i], pl->branch[i]);
+      cudaEventRecord(pl->ev[i], pl->branch[i]);
+      cudaStreamWaitEvent(pl->cap, pl->ev[i], 0);
+    }
+    x.launches = pht::tl_launches - l0;
+    if (cudaStreamEndCapture(pl->cap, &pl->graph) != cudaSuccess || !pl->graph) rc = PARAHT_ERR_CUDA;
+  }
+  if (!rc && cudaGraphInstantiate(&pl->exec, pl->graph, 0) != cudaSuccess) rc = PARAHT_ERR_CUDA;
+  if (rc) cudaGetLastError();
+  cudaSetDevice(prev);
+  if (rc) {
+    plan_free(pl);
+    return rc;
+  }
+  *plan = pl;
+  return 0;
+}
+
+extern "C" int paraht_batch_plan_launch(paraht_batch_plan pl, void* stream) {
+  if (!pl || pl->magic != kPlanMagic) return PARAHT_ERR_BAD_CTX;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(pl->device);
+  const cudaError_t e = cudaGraphLaunch(pl->exec, (cudaStream_t)stream);
+  cudaSetDevice(prev);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return PARAHT_ERR_CUDA;
+  }
+  return 0;
+}
+
+extern "C" int paraht_batch_plan_destroy(paraht_batch_plan pl) {
+  if (!pl || pl->magic != kPlanMagic) return PARAHT_ERR_BAD_CTX;
+  plan_free(pl);
+  return 0;
 }
 
 extern "C" int paraht_reduce_batched_d(paraht_ctx c, int count, const int* n, double* const* A, const int* lda,

@@ -20,6 +20,7 @@
 // PARAHT_FLAG_SPLIT.  The CTA's reflector workspace lives in a per-CTA slice of one device
 // buffer.
 #include <algorithm>
+#include <new>
 #include <numeric>
 #include <string.h>
 #include <vector>
@@ -217,35 +218,25 @@ bool batch_eligible(int n, int r, int p, int nq) {
   return (size_t)p * r <= 64;
 }
 
-// Reduces the eligible pencils `idx` of the batch with one persistent launch on stream s.
-// Returns 0 or a PARAHT_ERR_* code; the launch is asynchronous.
-int batch_run(Ctx& x, cudaStream_t s, const std::vector<int>& idx, const int* n, double* const* A, const int* lda,
-              double* const* B, const int* ldb, double* const* Q, const int* ldq, double* const* Z, const int* ldz,
-              const int* r, const int* p, const int* nq) {
-  const int count = (int)idx.size();
-  if (count == 0) return 0;
-  std::vector<BatchItem> items(count);
-  size_t wsd = 0;
+// Launch shape of one persistent launch over `count` pencils: shared memory (the largest body; the
+// RQ reflector copy of the right generation only if two CTAs still fit per SM), grid, and the
+// per-CTA workspace in doubles.
+static int batch_shape(Ctx& x, const BatchItem* items, int count, size_t& smem, int& grid, int& use_vr,
+                       size_t& wsd) {
+  wsd = 0;
   int Lmax = 0, rmax = 0, nqmax = 0;
   for (int k = 0; k < count; ++k) {
-    const int i = idx[k];
-    items[k] = BatchItem{A[i], B[i], Q[i], Z[i], n[i], lda[i], ldb[i], ldq[i], ldz[i], r[i], p[i], nq[i]};
-    wsd = std::max(wsd, batch_ws_doubles(n[i], r[i], p[i], nq[i]));
-    Lmax = std::max(Lmax, p[i] * r[i]);
-    rmax = std::max(rmax, r[i]);
-    nqmax = std::max(nqmax, nq[i]);
+    wsd = std::max(wsd, batch_ws_doubles(items[k].n, items[k].r, items[k].p, items[k].nq));
+    Lmax = std::max(Lmax, items[k].p * items[k].r);
+    rmax = std::max(rmax, items[k].r);
+    nqmax = std::max(nqmax, items[k].nq);
   }
-  // longest first: pencils sorted by decreasing n
-  std::vector<int> order(count);
-  std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return items[a].n > items[b].n; });
-  // shared memory: the largest body; the RQ reflector copy (rgen) only if two CTAs still fit per SM
   const size_t base = std::max({kLeftSmem, right_smem<64>(), s1_lgen_smem(Lmax, rmax), chase_smem_bytes(rmax, nqmax),
                                 sizeof(double) * 2 * (size_t)nqmax * nqmax});
   const size_t with_vr = std::max(base, s1_rgen_smem_vr(Lmax, rmax, true));
   const size_t without_vr = std::max(base, s1_rgen_smem_vr(Lmax, rmax, false));
-  const int use_vr = with_vr <= (size_t)x.max_smem / 2 - 1024 ? 1 : 0;
-  const size_t smem = use_vr ? with_vr : without_vr;
+  use_vr = with_vr <= (size_t)x.max_smem / 2 - 1024 ? 1 : 0;
+  smem = use_vr ? with_vr : without_vr;
   if (smem > (size_t)x.max_smem - 1024) return PARAHT_ERR_NOT_SUPPORTED;  // static __shared__ words too
   if (cudaFuncSetAttribute(k_batch_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
     cudaGetLastError();
@@ -257,35 +248,132 @@ int batch_run(Ctx& x, cudaStream_t s, const std::vector<int>& idx, const int* n,
     cudaGetLastError();
     per_sm = 1;
   }
-  const int grid = std::min(count, per_sm * std::max(1, x.num_sms));
-  // device buffer: items | order | queue counter | per-CTA workspace (256-byte aligned slices)
-  const size_t items_b = ((sizeof(BatchItem) * count + 255) / 256) * 256;
-  const size_t order_b = ((sizeof(int) * count + 255) / 256) * 256;
-  const size_t stride = ((wsd * sizeof(double) + 255) / 256) * 256;
-  const size_t need = items_b + order_b + 256 + stride * grid;
-  if (need > x.bws_bytes) {
+  grid = std::min(count, per_sm * std::max(1, x.num_sms));
+  return 0;
+}
+
+// Byte layout of a launch's device buffer: items | order | queue counter | per-CTA workspace
+// (256-byte aligned slices).
+struct BatchLayout {
+  size_t items_b, order_b, stride, total;
+};
+static BatchLayout batch_layout(int count, size_t wsd, int grid) {
+  BatchLayout l;
+  l.items_b = ((sizeof(BatchItem) * count + 255) / 256) * 256;
+  l.order_b = ((sizeof(int) * count + 255) / 256) * 256;
+  l.stride = ((wsd * sizeof(double) + 255) / 256) * 256;
+  l.total = l.items_b + l.order_b + 256 + l.stride * grid;
+  return l;
+}
+
+// Host image of the pencil table and the queue order (longest first: decreasing n).
+static void batch_table(const BatchItem* items, int count, const BatchLayout& l, std::vector<char>& host) {
+  std::vector<int> order(count);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return items[a].n > items[b].n; });
+  host.assign(l.items_b + l.order_b, 0);
+  memcpy(host.data(), items, sizeof(BatchItem) * count);
+  memcpy(host.data() + l.items_b, order.data(), sizeof(int) * count);
+}
+
+static void batch_enqueue_raw(char* d, const BatchLayout& l, int count, int grid, size_t smem, int use_vr,
+                              cudaStream_t s) {
+  int* dnext = (int*)(d + l.items_b + l.order_b);
+  cudaMemsetAsync(dnext, 0, sizeof(int), s);
+  count_launch();
+  k_batch_reduce<<<grid, kBatchThreads, smem, s>>>((const BatchItem*)d, (const int*)(d + l.items_b), count, dnext,
+                                                   (double*)(d + l.items_b + l.order_b + 256), l.stride / sizeof(double),
+                                                   use_vr);
+}
+
+// Reduces the eligible pencils `idx` of the batch with one persistent launch on stream s.
+// Returns 0 or a PARAHT_ERR_* code; the launch is asynchronous.
+int batch_run(Ctx& x, cudaStream_t s, const std::vector<int>& idx, const int* n, double* const* A, const int* lda,
+              double* const* B, const int* ldb, double* const* Q, const int* ldq, double* const* Z, const int* ldz,
+              const int* r, const int* p, const int* nq) {
+  const int count = (int)idx.size();
+  if (count == 0) return 0;
+  std::vector<BatchItem> items(count);
+  for (int k = 0; k < count; ++k) {
+    const int i = idx[k];
+    items[k] = BatchItem{A[i], B[i], Q[i], Z[i], n[i], lda[i], ldb[i], ldq[i], ldz[i], r[i], p[i], nq[i]};
+  }
+  size_t smem = 0, wsd = 0;
+  int grid = 0, use_vr = 0;
+  if (const int rc = batch_shape(x, items.data(), count, smem, grid, use_vr, wsd)) return rc;
+  const BatchLayout l = batch_layout(count, wsd, grid);
+  if (l.total > x.bws_bytes) {
     if (x.bws) cudaFree(x.bws);
     x.bws = nullptr;
     x.bws_bytes = 0;
-    if (cudaMalloc(&x.bws, need) != cudaSuccess) {
+    if (cudaMalloc(&x.bws, l.total) != cudaSuccess) {
       cudaGetLastError();
       return PARAHT_ERR_ALLOC;
     }
-    x.bws_bytes = need;
+    x.bws_bytes = l.total;
   }
-  char* d = (char*)x.bws;
-  BatchItem* ditems = (BatchItem*)d;
-  int* dorder = (int*)(d + items_b);
-  int* dnext = (int*)(d + items_b + order_b);
-  double* dws = (double*)(d + items_b + order_b + 256);
-  x.bhost.resize(items_b + order_b);
-  memcpy(x.bhost.data(), items.data(), sizeof(BatchItem) * count);
-  memcpy(x.bhost.data() + items_b, order.data(), sizeof(int) * count);
-  cudaMemcpyAsync(d, x.bhost.data(), items_b + order_b, cudaMemcpyHostToDevice, s);
-  cudaMemsetAsync(dnext, 0, sizeof(int), s);
-  count_launch();
-  k_batch_reduce<<<grid, kBatchThreads, smem, s>>>(ditems, dorder, count, dnext, dws, stride / sizeof(double), use_vr);
+  batch_table(items.data(), count, l, x.bhost);
+  cudaMemcpyAsync(x.bws, x.bhost.data(), l.items_b + l.order_b, cudaMemcpyHostToDevice, s);
+  batch_enqueue_raw((char*)x.bws, l, count, grid, smem, use_vr, s);
   return cudaGetLastError() == cudaSuccess ? 0 : PARAHT_ERR_CUDA;
+}
+
+// ---- plans: one bucket of pencils sharing (r, p, nq), with its own buffer and launch shape ----
+struct BatchBucket {
+  char* buf = nullptr;
+  BatchLayout l{};
+  int count = 0, grid = 0, use_vr = 0;
+  size_t smem = 0;
+};
+
+int batch_bucket_create(Ctx& x, const std::vector<int>& idx, const int* n, double* const* A, const int* lda,
+                        double* const* B, const int* ldb, double* const* Q, const int* ldq, double* const* Z,
+                        const int* ldz, const int* r, const int* p, const int* nq, void** out) {
+  *out = nullptr;
+  auto* b = new (std::nothrow) BatchBucket();
+  if (!b) return PARAHT_ERR_ALLOC;
+  b->count = (int)idx.size();
+  std::vector<BatchItem> items(b->count);
+  for (int k = 0; k < b->count; ++k) {
+    const int i = idx[k];
+    items[k] = BatchItem{A[i], B[i], Q[i], Z[i], n[i], lda[i], ldb[i], ldq[i], ldz[i], r[i], p[i], nq[i]};
+  }
+  size_t wsd = 0;
+  int rc = batch_shape(x, items.data(), b->count, b->smem, b->grid, b->use_vr, wsd);
+  if (!rc) {
+    b->l = batch_layout(b->count, wsd, b->grid);
+    if (cudaMalloc((void**)&b->buf, b->l.total) != cudaSuccess) {
+      cudaGetLastError();
+      b->buf = nullptr;
+      rc = PARAHT_ERR_ALLOC;
+    }
+  }
+  if (!rc) {
+    std::vector<char> host;
+    batch_table(items.data(), b->count, b->l, host);
+    if (cudaMemcpy(b->buf, host.data(), host.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+      cudaGetLastError();
+      rc = PARAHT_ERR_CUDA;
+    }
+  }
+  if (rc) {
+    batch_bucket_destroy(b);
+    return rc;
+  }
+  *out = b;
+  return 0;
+}
+
+void batch_bucket_enqueue(const void* bucket, cudaStream_t s) {
+  const auto* b = static_cast<const BatchBucket*>(bucket);
+  batch_enqueue_raw(b->buf, b->l, b->count, b->grid, b->smem, b->use_vr, s);
+}
+
+void batch_bucket_destroy(void* bucket) {
+  auto* b = static_cast<BatchBucket*>(bucket);
+  if (!b) return;
+  if (b->buf) cudaFree(b->buf);
+  delete b;
 }
 
 }  // namespace pht

@@ -134,5 +134,12 @@ bool batch_eligible(int n, int r, int p, int nq);
 int batch_run(Ctx& x, cudaStream_t s, const std::vector<int>& idx, const int* n, double* const* A, const int* lda,
               double* const* B, const int* ldb, double* const* Q, const int* ldq, double* const* Z, const int* ldz,
               const int* r, const int* p, const int* nq);
+// A bucket of a batch plan (batched.cu): the pencils idx[], all taken by the persistent kernel, with
+// their table uploaded to a buffer of their own; enqueue = queue reset + one persistent launch.
+int batch_bucket_create(Ctx& x, const std::vector<int>& idx, const int* n, double* const* A, const int* lda,
+                        double* const* B, const int* ldb, double* const* Q, const int* ldq, double* const* Z,
+                        const int* ldz, const int* r, const int* p, const int* nq, void** bucket);
+void batch_bucket_enqueue(const void* bucket, cudaStream_t s);
+void batch_bucket_destroy(void* bucket);
 
 }  // namespace pht

@@ -111,3 +111,45 @@ def test_batched_rejects_bad_arguments(ctx):
         ctx.reduce_batched_d([10], [0], [10], [0], [10], [0], [10], [0], [10], [4], [2], [2])
     assert e.value.status == -3
     ctx.reduce_batched_d([], [], [], [], [], [], [], [], [], [], [], [])  # empty batch is a no-op
+
+
+def test_batch_plan_graph_replays_bitwise(ctx):
+    """paraht_batch_plan_*: the persistent launches captured as a CUDA graph (one bucket per
+    (r, p, nq)) and replayed twice on new values in the same arrays give paraht_reduce_d's bits."""
+    torch = pytest.importorskip("torch")
+    cases = [c for c in CASES if c[1] * c[2] <= 64]  # the pencils the persistent kernel takes
+    ns = [c[0] for c in cases]
+    ld = [max(1, n) for n in ns]
+    rs, ps, nqs = [c[1] for c in cases], [c[2] for c in cases], [c[3] for c in cases]
+    assert len(set(zip(rs, ps, nqs))) >= 3  # several buckets
+    dev = [[torch.zeros((max(n, 1), max(n, 1)), dtype=torch.float64, device="cuda") for _ in range(4)] for n in ns]
+    ptr = lambda j: [d[j].data_ptr() for d in dev]  # noqa: E731
+    plan = ctx.batch_plan(ns, ptr(0), ld, ptr(1), ld, ptr(2), ld, ptr(3), ld, rs, ps, nqs)
+    stream = torch.cuda.Stream()
+    for rep in range(2):  # two replays on different inputs
+        ref = []
+        for k, (n, r, p, nq, dist) in enumerate(cases):
+            A0, B0 = make(max(n, 2), dist, seed=7000 + 13 * rep + k)
+            A0, B0 = A0[:n, :n].copy(order="F"), np.triu(B0[:n, :n]).copy(order="F")
+            for j, X in enumerate((A0, B0, identity(n), identity(n))):
+                dev[k][j].copy_(_dev(torch, X))
+            ref.append(_run_single(torch, ctx, A0, B0, r, p, nq, 0))
+        torch.cuda.synchronize()
+        plan.launch(stream.cuda_stream)
+        stream.synchronize()
+        for k in range(len(cases)):
+            for X, D in zip(ref[k], dev[k]):
+                assert np.array_equal(X, D.cpu().numpy().T)
+    plan.close()
+
+
+def test_batch_plan_rejects_what_the_persistent_kernel_cannot_take(ctx):
+    torch = pytest.importorskip("torch")
+    X = torch.zeros((64, 64), dtype=torch.float64, device="cuda")
+    p = X.data_ptr()
+    for n, r, pp, nq, flags in ((64, 16, 8, 16, 0),            # p r = 128
+                                (2000, 16, 4, 16, 0),          # n > PARAHT_BATCH_MAX_N
+                                (64, 16, 4, 16, ph.PARAHT_FLAG_SPLIT)):
+        with pytest.raises(ph.ParahtError) as e:
+            ctx.batch_plan([n], [p], [n], [p], [n], [p], [n], [p], [n], [r], [pp], [nq], flags)
+        assert e.value.status == -1005
