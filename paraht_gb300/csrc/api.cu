@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <array>
 #include <cctype>
+#include <map>
 #include <atomic>
 #include <mutex>
 #include <new>
@@ -139,6 +140,25 @@ __global__ void k_check_finite(int n, const double* X, int ldx, int* flag) {
   const int j = blockIdx.x;
   for (int i = threadIdx.x; i < n; i += blockDim.x)
     if (!isfinite(X[(size_t)i + (size_t)j * ldx])) atomicOr(flag, 1);
+}
+
+int smem_at_least(const void* func, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, size_t> granted;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return PARAHT_ERR_CUDA;
+  }
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& g = granted[{func, dev}];
+  if (bytes <= g) return 0;
+  if (cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return PARAHT_ERR_CUDA;
+  }
+  g = bytes;
+  return 0;
 }
 
 int check_finite(cudaStream_t s, int n, const double* A, int lda, const double* B, int ldb, int* dflag) {

@@ -238,10 +238,7 @@ static int batch_shape(Ctx& x, const BatchItem* items, int count, size_t& smem, 
   use_vr = with_vr <= (size_t)x.max_smem / 2 - 1024 ? 1 : 0;
   smem = use_vr ? with_vr : without_vr;
   if (smem > (size_t)x.max_smem - 1024) return PARAHT_ERR_NOT_SUPPORTED;  // static __shared__ words too
-  if (cudaFuncSetAttribute(k_batch_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
-    cudaGetLastError();
-    return PARAHT_ERR_CUDA;
-  }
+  if (const int rc = smem_at_least((const void*)k_batch_reduce, smem)) return rc;
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_reduce, kBatchThreads, smem) != cudaSuccess ||
       per_sm < 1) {

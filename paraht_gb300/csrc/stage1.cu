@@ -359,6 +359,7 @@ static size_t right_gen_small(int L, int nb) {
 }
 static size_t right_gen_big(int L, int nb) { return sizeof(double) * ((size_t)(L + 1) * L + (size_t)nb * (L + 1)); }
 
+int s1_gen_grant();
 void launch_s1_lgen(cudaStream_t s, double* A, int lda, const S1Panel& P, double* VL, double* TL);
 void launch_s1_rgen(cudaStream_t s, const double* B, int ldb, const S1Panel& P, int o, double* VRc, double* TR);
 
@@ -403,8 +404,12 @@ int s1_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
   const size_t rsm = r_in_smem ? rsm_small + right_gen_big(L, nb) : rsm_small;
   if ((!fast_l && lsm > (size_t)ctx.max_smem) || (!fast_r && rsm_small > (size_t)ctx.max_smem))
     return PARAHT_ERR_NOT_SUPPORTED;
-  if (!fast_l) cudaFuncSetAttribute(k_s1_left_gen, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsm);
-  if (!fast_r) cudaFuncSetAttribute(k_s1_right_gen, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm);
+  if (fast_l || fast_r)
+    if (const int rc = s1_gen_grant()) return rc;
+  if (!fast_l)
+    if (const int rc = smem_at_least((const void*)k_s1_left_gen, lsm)) return rc;
+  if (!fast_r)
+    if (const int rc = smem_at_least((const void*)k_s1_right_gen, rsm)) return rc;
 
   // split-precision bulk updates (split_apply.cuh) where the op shapes fit; one operand region
   // per launch site: 0 B left, 1 A left, 2 Q, 3 remaining B rows, 4 A right, 5 Z right

@@ -18,22 +18,19 @@ __global__ void __launch_bounds__(512) k_s1_rgen(const double* __restrict__ B, i
   s1_rgen_body(B, ldb, P, o, VRc, TR, use_vr, (int)blockDim.x, sm);
 }
 
+// Grants both generation kernels the full 227 KB of dynamic shared memory on the current device
+// (once per process and device in effect: smem_at_least only calls the runtime when the limit grows).
+int s1_gen_grant() {
+  if (const int rc = smem_at_least((const void*)k_s1_lgen, 227 * 1024)) return rc;
+  return smem_at_least((const void*)k_s1_rgen, 227 * 1024);
+}
+
 void launch_s1_lgen(cudaStream_t s, double* A, int lda, const S1Panel& P, double* VL, double* TL) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_s1_lgen, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    attr = true;
-  }
   count_launch();
   k_s1_lgen<<<1, s1_lgen_threads(P.nb), s1_lgen_smem(P.L, P.nb), s>>>(A, lda, P, VL, TL);
 }
 
 void launch_s1_rgen(cudaStream_t s, const double* B, int ldb, const S1Panel& P, int o, double* VRc, double* TR) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_s1_rgen, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    attr = true;
-  }
   static int max_smem = -1;
   if (max_smem < 0) {
     int dev = 0;

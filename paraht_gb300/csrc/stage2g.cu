@@ -185,7 +185,7 @@ int s2g_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, 
     }
   const size_t stair_smem = sizeof(double) * 128 * (size_t)(ldu + 1);
   if (stair_smem > 48 * 1024)
-    cudaFuncSetAttribute(k_s2g_stair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stair_smem);
+    if (const int rc = smem_at_least((const void*)k_s2g_stair, stair_smem)) return rc;
   int k = 0;
   for (int J = 1; J <= n - 2; J += nq, ++k) {
     const int nblocks = (n - J + r - 1) / r;

@@ -113,11 +113,16 @@ def test_batched_rejects_bad_arguments(ctx):
     ctx.reduce_batched_d([], [], [], [], [], [], [], [], [], [], [], [])  # empty batch is a no-op
 
 
-def test_batch_plan_graph_replays_bitwise(ctx):
+@pytest.mark.parametrize("order", ["given", "reversed"])
+def test_batch_plan_graph_replays_bitwise(ctx, order):
     """paraht_batch_plan_*: the persistent launches captured as a CUDA graph (one bucket per
-    (r, p, nq)) and replayed twice on new values in the same arrays give paraht_reduce_d's bits."""
+    (r, p, nq)) and replayed twice on new values in the same arrays give paraht_reduce_d's bits.
+    Both bucket orders: a bucket with smaller tiles created after a larger one must not lower the
+    shared-memory limit the larger one's captured launch needs."""
     torch = pytest.importorskip("torch")
     cases = [c for c in CASES if c[1] * c[2] <= 64]  # the pencils the persistent kernel takes
+    if order == "reversed":
+        cases = cases[::-1]
     ns = [c[0] for c in cases]
     ld = [max(1, n) for n in ns]
     rs, ps, nqs = [c[1] for c in cases], [c[2] for c in cases], [c[3] for c in cases]
