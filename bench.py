@@ -111,6 +111,8 @@ def parse(argv=None):
                     help="wall-clock budget of the whole run in seconds, from process start")
     ap.add_argument("--warmup-n", type=int, default=2000, help="size of the reduced-size warm-up steps")
     ap.add_argument("--phases", action="store_true", help="one extra serialised step for the per-phase times")
+    ap.add_argument("--chain", action="store_true",
+                    help="one extra overlapped step with the critical-path share of each phase (PARAHT_FLAG_TIME_CHAIN)")
     ap.add_argument("--save-stage1", default="", help="after the run, save this pencil's stage-1 output here")
     ap.add_argument("--stage2-from", default="", help="time stage 2 alone on a saved stage-1 output")
     return ap.parse_args(argv)
@@ -638,7 +640,9 @@ def run_pencil(args, rank: int, world: int, local: int):
             fst = ctx.kernel_stats()["stage2"]
             fp64 = {"seconds": t_f, "r": fr, "p": fp, "nq": fnq, "stage2": args.fp64_stage2, "launches": ctx.launch_count(),
                     "effective_gflops": flops_nominal(n) / t_f / 1e9,
-                    "op_list_kernel": {"kernel": "k_apply_left/k_apply_right<GeoS2> (FP64 compact-WY op lists)",
+                    "op_list_kernel": {"kernel": ("k_apply_left/k_apply_right<GeoS2G> (FP64 dense op lists)"
+                                                  if args.fp64_stage2 == "givens" else
+                                                  "k_apply_left/k_apply_right<GeoS2> (FP64 compact-WY op lists)"),
                                        "achieved_tflops": fst["flops"] / fst["seconds"] / 1e12 if fst["seconds"] > 0 else None,
                                        "peak_tflops": fp64_peak,
                                        "peak_source": "cuBLAS DGEMM 8192^3 measured in this run, of measured",
@@ -699,6 +703,11 @@ def run_pencil(args, rank: int, world: int, local: int):
         restore()
         launch(work, n, (r, p, nq), flags | ph.PARAHT_FLAG_TIME_COMPONENTS)
         phases = {k: round(v, 4) for k, v in ctx.phase_times().items()}
+    chain = None
+    if args.chain:  # the phase marks on each stage's critical-path stream, side streams overlapped
+        restore()
+        launch(work, n, (r, p, nq), flags | ph.PARAHT_FLAG_TIME_CHAIN)
+        chain = {k: round(v, 4) for k, v in ctx.phase_times().items()}
 
     # roofline of the dominant kernel: the compact-WY op-list kernel of stage 2 (bulk and
     # lookahead updates), timed launch by launch with CUDA events on its streams during the timed
@@ -720,8 +729,11 @@ def run_pencil(args, rank: int, world: int, local: int):
         achieved = 43.0 * fp64eq if fp64eq else None
         roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                     "frac": achieved / peak if achieved else None, "traffic": None,
-                    "kernel": "k_ws_apply<GeoS2> (split-precision compact-WY op lists, FP16 digit MMAs)",
-                    "work": "4 len k FP64-equivalent flops per strip row per op, x43 FP16 digit-pair products",
+                    "kernel": ("k_ws_apply<GeoS2G> (split-precision op lists of the Givens stage 2: dense "
+                               "(r+nq)^2 blocks, FP16 digit MMAs)" if args.stage2 == "givens" else
+                               "k_ws_apply<GeoS2> (split-precision compact-WY op lists, FP16 digit MMAs)"),
+                    "work": ("2 len^2 FP64-equivalent flops per strip row per dense op" if args.stage2 == "givens" else
+                             "4 len k FP64-equivalent flops per strip row per op") + ", x43 FP16 digit-pair products",
                     "peak_source": ("MEASURED_PEAKS.json bf16_tflops (FP16 and BF16 mma run at the same rate), of measured"
                                     if measured else "1.9 PFLOP/s BF16 burst, of fallback (no MEASURED_PEAKS.json)"),
                     "fp64_equivalent_tflops": fp64eq,
@@ -737,7 +749,9 @@ def run_pencil(args, rank: int, world: int, local: int):
     else:
         roofline = {"bound": "fp64", "achieved": fp64eq, "peak": fp64_peak, "unit": "TFLOP/s",
                     "frac": fp64eq / fp64_peak if fp64eq else None, "traffic": None,
-                    "kernel": "k_apply_left/k_apply_right<GeoS2> (FP64 compact-WY op lists)",
+                    "kernel": ("k_apply_left/k_apply_right<GeoS2G> (FP64 dense op lists of the Givens stage 2)"
+                               if args.stage2 == "givens" else
+                               "k_apply_left/k_apply_right<GeoS2> (FP64 compact-WY op lists)"),
                     "work": "4 len k flops per strip row per op",
                     "peak_source": "cuBLAS DGEMM 8192^3 measured in this run, of measured",
                     "aggregate": {"busy_s_per_step": s2["busy_seconds"] / max(1, steps_done),
@@ -805,6 +819,8 @@ def run_pencil(args, rank: int, world: int, local: int):
             line["check"] = check
         if phases:
             line["phases_s"] = phases
+        if chain:
+            line["critical_path_s"] = chain
         print(json.dumps(line), flush=True)
     if dist_on:
         import torch.distributed as td

@@ -60,6 +60,10 @@ extern "C" {
 
 #define PARAHT_FLAG_GIVENS 128     /* stage 2 by Givens rotations (rht2ht_givens, src/rht2ht.f90:696-1344)
                                          instead of small reflectors; needs r <= 32 and r + nq <= 64 */
+#define PARAHT_FLAG_TIME_CHAIN 256 /* record the phase times on the critical-path stream of each stage
+                                      without serialising the side streams: the phases then add up to the
+                                      overlapped call's device time, each one holding the time the
+                                      critical path spent in it, its waits for side streams included */
 
 typedef struct paraht_ctx_s* paraht_ctx;
 
@@ -68,7 +72,8 @@ int paraht_ctx_create(paraht_ctx* ctx, int device);
 int paraht_ctx_destroy(paraht_ctx ctx);
 /* Use an existing cudaStream_t (passed as void*); NULL selects the context's own stream. */
 int paraht_ctx_set_stream(paraht_ctx ctx, void* stream);
-/* Phase times of the last call, in seconds, when PARAHT_FLAG_TIME_COMPONENTS was set:
+/* Phase times of the last call, in seconds, when PARAHT_FLAG_TIME_COMPONENTS (phases run one after
+ * the other) or PARAHT_FLAG_TIME_CHAIN (critical-path shares of the overlapped run) was set:
  *   [0] stage-1 left generation  [1] stage-1 right generation  [2] stage-1 multiplications
  *   [3] stage-2 generation       [4] stage-2 lookahead          [5] stage-2 application
  *   [6] host<->device copies (host entry points only)             [7] total device time

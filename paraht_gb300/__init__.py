@@ -26,13 +26,14 @@ import numpy as np
 
 from ._lib import (PARAHT_BATCH_MAX_N, PARAHT_FLAG_BATCH_LOOP, PARAHT_FLAG_CHECK_FINITE, PARAHT_FLAG_GIVENS,
                    PARAHT_FLAG_KERNEL_TIMES, PARAHT_FLAG_NO_ZERO_FILL, PARAHT_FLAG_SEQUENTIAL, PARAHT_FLAG_SPLIT,
-                   PARAHT_FLAG_TIME_COMPONENTS, ParahtError, check, lib)
+                   PARAHT_FLAG_TIME_CHAIN, PARAHT_FLAG_TIME_COMPONENTS, ParahtError, check, lib)
 
 __all__ = [
     "ab2rht_simple", "rht2ht_householder", "rht2ht_givens", "reduce", "ht", "gghd3", "Context", "BatchPlan",
     "ParahtError",
     "PARAHT_FLAG_TIME_COMPONENTS", "PARAHT_FLAG_CHECK_FINITE", "PARAHT_FLAG_SPLIT", "PARAHT_FLAG_NO_ZERO_FILL",
     "PARAHT_FLAG_SEQUENTIAL", "PARAHT_FLAG_KERNEL_TIMES", "PARAHT_FLAG_BATCH_LOOP", "PARAHT_FLAG_GIVENS",
+    "PARAHT_FLAG_TIME_CHAIN",
     "PARAHT_BATCH_MAX_N",
 ]
 

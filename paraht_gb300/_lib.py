@@ -18,6 +18,7 @@ PARAHT_FLAG_SEQUENTIAL = 16
 PARAHT_FLAG_KERNEL_TIMES = 32
 PARAHT_FLAG_BATCH_LOOP = 64
 PARAHT_FLAG_GIVENS = 128
+PARAHT_FLAG_TIME_CHAIN = 256
 PARAHT_BATCH_MAX_N = 1024
 
 ERRORS = {

@@ -385,7 +385,8 @@ static int run_device_on(Ctx& x, int which, int n, double* A, int lda, double* B
     if (!x.split_region(0, ops, sizeof(pht::SplitOpData))) return PARAHT_ERR_ALLOC;
   }
   const long long launches0 = pht::tl_launches;
-  const bool timed = flags & PARAHT_FLAG_TIME_COMPONENTS;
+  const bool timed = flags & (PARAHT_FLAG_TIME_COMPONENTS | PARAHT_FLAG_TIME_CHAIN);
+  x.timer.serial = (flags & PARAHT_FLAG_TIME_COMPONENTS) != 0;
   const bool ktimes = flags & PARAHT_FLAG_KERNEL_TIMES;
   for (double& v : x.kstats) v = 0.0;
   if (ktimes) {
@@ -838,7 +839,8 @@ extern "C" int paraht_reduce_batched_d(paraht_ctx c, int count, const int* n, do
   cudaGetDevice(&prev);
   cudaSetDevice(x.device);
   x.launches = 0;
-  const int single_flags = flags & ~(PARAHT_FLAG_TIME_COMPONENTS | PARAHT_FLAG_BATCH_LOOP | PARAHT_FLAG_KERNEL_TIMES);
+  const int single_flags =
+      flags & ~(PARAHT_FLAG_TIME_COMPONENTS | PARAHT_FLAG_TIME_CHAIN | PARAHT_FLAG_BATCH_LOOP | PARAHT_FLAG_KERNEL_TIMES);
   std::vector<int> small, large;
   for (int i = 0; i < count; ++i) {
     if (n[i] == 0) continue;
@@ -985,7 +987,7 @@ static int gghd3_device(Ctx& x, char compq, char compz, int n, int ilo, int ihi,
     pht::set_identity(x.stream, m, Zs, m);
     const size_t o = (size_t)(ilo - 1);
     rc = run_device(x, 3, m, A + o + o * lda, lda, B + o + o * ldb, ldb, Qs, m, Zs, m, r, p, nq,
-                    flags & ~(PARAHT_FLAG_TIME_COMPONENTS | PARAHT_FLAG_KERNEL_TIMES));
+                    flags & ~(PARAHT_FLAG_TIME_COMPONENTS | PARAHT_FLAG_TIME_CHAIN | PARAHT_FLAG_KERNEL_TIMES));
     if (!rc) {
       auto copy_back = [&](double* dst, int ldd, int rows, int cols) {
         cudaMemcpy2DAsync(dst, (size_t)ldd * sizeof(double), Tm, (size_t)rows * sizeof(double),

@@ -16,6 +16,7 @@ struct PhaseTimer {
   std::vector<int> phase;
   size_t used = 0;
   int offset = 0;  // phase index offset (stage 2 phases start at 3)
+  bool serial = true;  // the stages run their side-stream work on the timed stream
   void reset(int off) {
     used = 0;
     phase.clear();
@@ -67,7 +68,8 @@ struct Ctx {
   cudaStream_t crit = nullptr;
   cudaEvent_t ev_enter = nullptr, ev_exit = nullptr;
   cudaEvent_t ev_a = nullptr, ev_b = nullptr;
-  cudaEvent_t ev_s2[4] = {};        // stage-2 bulk chains: operands prepared, and the joins of A, Q, Z
+  cudaEvent_t ev_s2[6] = {};        // stage-2 bulk chains: operands prepared, A joined to B, then the
+                                    // Q and Z lists of the groups using store 0 ([2], [3]) and 1 ([4], [5])
   cudaEvent_t ev[8] = {};           // stage-1 dependency events
   int sequential_chase = 0;         // 1: run stage-2 sweeps one after the other in one CTA
   long long spin_limit = 1ll << 24;  // polls before a device-side wait gives up

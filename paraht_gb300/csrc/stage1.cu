@@ -377,7 +377,7 @@ int s1_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
            PhaseTimer* timer) {
   if (n - nb - 1 < 1) return 0;  // ab2rht.f90:71: empty panel loop
   const int L = p * nb;
-  const bool serial = timer != nullptr;
+  const bool serial = timer != nullptr && timer->serial;
   cudaStream_t sA = ctx.stream, sB = serial ? sA : ctx.side, sC = serial ? sA : ctx.side2;
   const size_t nblk0 = s1_nblk0(n, nb, p);
   double* ws = (double*)ctx.workspace(s1_workspace_bytes(n, nb, p));

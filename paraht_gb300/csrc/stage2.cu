@@ -75,8 +75,8 @@ int s2_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
   // (the reference's priority-100 / priority-1 tasks).  With time_components everything runs
   // on the main stream so the phases can be timed separately (the reference inserts taskwaits).
   cudaStream_t sg = ctx.stream;
-  cudaStream_t su = (timer || ctx.sequential_chase) ? ctx.stream : ctx.side;
-  const bool one_bulk = timer || ctx.sequential_chase;
+  const bool one_bulk = (timer && timer->serial) || ctx.sequential_chase;
+  cudaStream_t su = one_bulk ? ctx.stream : ctx.side;
   cudaStream_t sa = one_bulk ? su : ctx.side2, sq = one_bulk ? su : ctx.side3, sz = one_bulk ? su : ctx.side4;
   if (su != sg) {
     cudaEventRecord(ctx.ev_a, sg);
@@ -98,6 +98,11 @@ int s2_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
     const int nblocks = (n - J + r - 1) / r;
     const int nz = std::min(nb0, nblocks + 2);
     const S2Store& St = S[k & 1];
+    if (k >= 2 && su != sg) {  // the Q and Z lists of group k-2 read this store
+      if (timer) timer->mark(sg, 2);
+      cudaStreamWaitEvent(sg, ctx.ev_s2[2 + 2 * (k & 1)], 0);
+      cudaStreamWaitEvent(sg, ctx.ev_s2[3 + 2 * (k & 1)], 0);
+    }
     if (timer) timer->mark(sg, 0);
     cudaMemsetAsync(St.U, 0, sizeof(double) * (size_t)ldu * nq * nz, sg);
     cudaMemsetAsync(St.V, 0, sizeof(double) * (size_t)ldu * nq * nz, sg);
@@ -107,8 +112,11 @@ int s2_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
     s2_launch_chase(sg, A, lda, B, ldb, n, J, r, nq, St, sync, ctx.sequential_chase, ctx.spin_limit);
     count_launch();
     k_s2_form_t<<<dim3(nblocks, 1), 128, sizeof(double) * 2 * nq * nq, sg>>>(n, J, r, nq, nblocks, St);
+    if (k > 0 && su != sg) {  // lookahead k after the A and B lists of group k-1
+      if (timer) timer->mark(sg, 2);
+      cudaStreamWaitEvent(sg, ctx.ev_b, 0);
+    }
     if (timer) timer->mark(sg, 1);
-    if (k > 0 && su != sg) cudaStreamWaitEvent(sg, ctx.ev_b, 0);  // lookahead k after bulk k-1
     GeoS2 g{St, n, J, r, nq, nblocks, kLaRight};
     g.blk = sp ? 1 : 0;  // split kernel: one op per block, row staircase through range()
     apply_right_any(reg[4], B, ldb, J, n - 1, g, nblocks, sg);  // rows >= istart >= jblock+1
@@ -146,15 +154,22 @@ int s2_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
     apply_left_any(reg[1], A, lda, J, n - 1, gl, nblocks, sa, false);
     apply_right_any(reg[2], Q, ldq, 0, n - 1, gq, nblocks, sq);
     apply_right_any(reg[3], Z, ldz, 0, n - 1, gz, nblocks, sz);
-    if (su != sa) {  // join the four chains on su
+    if (su != sa) {  // A joins B (the next lookahead's dependency); Q and Z run on
       cudaEventRecord(ctx.ev_s2[1], sa);
-      cudaEventRecord(ctx.ev_s2[2], sq);
-      cudaEventRecord(ctx.ev_s2[3], sz);
-      for (int i = 1; i < 4; ++i) cudaStreamWaitEvent(su, ctx.ev_s2[i], 0);
+      cudaStreamWaitEvent(su, ctx.ev_s2[1], 0);
+      cudaEventRecord(ctx.ev_s2[2 + 2 * (k & 1)], sq);
+      cudaEventRecord(ctx.ev_s2[3 + 2 * (k & 1)], sz);
     }
     if (su != sg) cudaEventRecord(ctx.ev_b, su);
   }
-  if (su != sg) cudaStreamWaitEvent(sg, ctx.ev_b, 0);
+  if (su != sg) {  // join; the Q and Z streams run in order, so their last group's events suffice
+    if (timer) timer->mark(sg, 2);
+    cudaStreamWaitEvent(sg, ctx.ev_b, 0);
+    if (k > 0) {
+      cudaStreamWaitEvent(sg, ctx.ev_s2[2 + 2 * ((k - 1) & 1)], 0);
+      cudaStreamWaitEvent(sg, ctx.ev_s2[3 + 2 * ((k - 1) & 1)], 0);
+    }
+  }
   if (timer) timer->mark(sg, -1);
   return 0;
 }

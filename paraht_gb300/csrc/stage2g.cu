@@ -166,7 +166,7 @@ int s2g_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, 
   sync.ticket = sync.prog + (nq + 1);
   sync.status = ctx.dstatus;
   cudaStream_t sg = ctx.stream;
-  const bool one_bulk = timer || ctx.sequential_chase;
+  const bool one_bulk = (timer && timer->serial) || ctx.sequential_chase;
   cudaStream_t su = one_bulk ? sg : ctx.side, sa = one_bulk ? sg : ctx.side2, sq = one_bulk ? sg : ctx.side3,
                sz = one_bulk ? sg : ctx.side4;
   set_identity(sg, ldu, ident, ldu);
@@ -190,14 +190,22 @@ int s2g_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, 
   for (int J = 1; J <= n - 2; J += nq, ++k) {
     const int nblocks = (n - J + r - 1) / r;
     const S2GStore& St = S[k & 1];
+    if (k >= 2 && su != sg) {  // the Q and Z lists of group k-2 read this store
+      if (timer) timer->mark(sg, 2);
+      cudaStreamWaitEvent(sg, ctx.ev_s2[2 + 2 * (k & 1)], 0);
+      cudaStreamWaitEvent(sg, ctx.ev_s2[3 + 2 * (k & 1)], 0);
+    }
     if (timer) timer->mark(sg, 0);
     count_launch();
     k_s2g_init<<<nblocks, 256, 0, sg>>>(St);
     s2g_launch_chase(sg, A, lda, B, ldb, n, J, r, nq, St, sync, ctx.sequential_chase, ctx.spin_limit);
     count_launch();
     k_s2g_form<<<nblocks, 256, 0, sg>>>(St);
+    if (k > 0 && su != sg) {  // lookahead k after the A and B lists of group k-1
+      if (timer) timer->mark(sg, 2);
+      cudaStreamWaitEvent(sg, ctx.ev_b, 0);
+    }
     if (timer) timer->mark(sg, 1);
-    if (k > 0 && su != sg) cudaStreamWaitEvent(sg, ctx.ev_b, 0);  // lookahead k after bulk k-1
     GeoS2G g{St, n, J, r, nq, nblocks, kGLaLeftB};
     launch_stair(sg, B, ldb, n, J, r, nq, nblocks, St, 0);
     apply_left_any(reg[4], B, ldb, J, n - 1, g, nblocks, sg);
@@ -230,15 +238,22 @@ int s2g_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, 
     apply_left_any(reg[1], A, lda, J, n - 1, gl, nblocks, sa, false);
     apply_right_any(reg[2], Q, ldq, 0, n - 1, gq, nblocks, sq);
     apply_right_any(reg[3], Z, ldz, 0, n - 1, gz, nblocks, sz);
-    if (su != sa) {
+    if (su != sa) {  // A joins B (the next lookahead's dependency); Q and Z run on
       cudaEventRecord(ctx.ev_s2[1], sa);
-      cudaEventRecord(ctx.ev_s2[2], sq);
-      cudaEventRecord(ctx.ev_s2[3], sz);
-      for (int i = 1; i < 4; ++i) cudaStreamWaitEvent(su, ctx.ev_s2[i], 0);
+      cudaStreamWaitEvent(su, ctx.ev_s2[1], 0);
+      cudaEventRecord(ctx.ev_s2[2 + 2 * (k & 1)], sq);
+      cudaEventRecord(ctx.ev_s2[3 + 2 * (k & 1)], sz);
     }
     if (su != sg) cudaEventRecord(ctx.ev_b, su);
   }
-  if (su != sg) cudaStreamWaitEvent(sg, ctx.ev_b, 0);
+  if (su != sg) {  // join; the Q and Z streams run in order, so their last group's events suffice
+    if (timer) timer->mark(sg, 2);
+    cudaStreamWaitEvent(sg, ctx.ev_b, 0);
+    if (k > 0) {
+      cudaStreamWaitEvent(sg, ctx.ev_s2[2 + 2 * ((k - 1) & 1)], 0);
+      cudaStreamWaitEvent(sg, ctx.ev_s2[3 + 2 * ((k - 1) & 1)], 0);
+    }
+  }
   if (timer) timer->mark(sg, -1);
   return 0;
 }

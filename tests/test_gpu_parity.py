@@ -88,6 +88,27 @@ def test_reduce_end_to_end(oracle, ctx, n, r, p, nq, dist):
     assert t["total"] > 0 and t["s1_genleft"] > 0 and t["s2_gen"] > 0
 
 
+@pytest.mark.parametrize("flags", [0, ph.PARAHT_FLAG_SPLIT, ph.PARAHT_FLAG_SPLIT | ph.PARAHT_FLAG_GIVENS])
+def test_time_chain_keeps_results_and_adds_up(ctx, flags):
+    """PARAHT_FLAG_TIME_CHAIN times the phases on each stage's critical-path stream with the side
+    streams still overlapped: bitwise the untimed results, and the six phases add up to the
+    device time between the stages' first and last marks (within the total)."""
+    n, r, p, nq = 600, 16, 4, 16
+    A0, B0 = make(n)
+    out = []
+    for f in (flags, flags | ph.PARAHT_FLAG_TIME_CHAIN):
+        A, B = copies(A0, B0)
+        Q, Z = identity(n), identity(n)
+        ctx.reduce_host(A, B, Q, Z, r, p, nq, flags=f)
+        out.append((A, B, Q, Z))
+    for X, Y in zip(*out):
+        assert np.array_equal(X, Y)
+    t = ctx.phase_times()
+    parts = sum(t[k] for k in ("s1_genleft", "s1_genright", "s1_mul", "s2_gen", "s2_lookahead", "s2_application"))
+    assert t["s1_genright"] > 0 and t["s2_gen"] > 0
+    assert 0.5 * t["total"] < parts <= 1.01 * t["total"]
+
+
 @pytest.mark.parametrize("n", [1, 2, 3, 4, 6, 9])
 def test_tiny_sizes(oracle, n):
     r, p, nq = 2, 2, 2

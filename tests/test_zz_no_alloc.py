@@ -121,7 +121,7 @@ def test_noalloc_rejects_oversize_and_unsupported_flags():
                              dev[3].data_ptr(), n, 16, 16)
     assert e.value.status == ERR_TOO_LARGE
     m = 64
-    for f in (ph.PARAHT_FLAG_SPLIT, ph.PARAHT_FLAG_TIME_COMPONENTS, ph.PARAHT_FLAG_KERNEL_TIMES,
+    for f in (ph.PARAHT_FLAG_SPLIT, ph.PARAHT_FLAG_TIME_COMPONENTS, ph.PARAHT_FLAG_TIME_CHAIN, ph.PARAHT_FLAG_KERNEL_TIMES,
               ph.PARAHT_FLAG_BATCH_LOOP, 1 << 20):
         with pytest.raises(ph.ParahtError) as e:
             ctx.rht2ht_d_noalloc(m, dev[0].data_ptr(), m, dev[1].data_ptr(), m, dev[2].data_ptr(), m,
