@@ -26,8 +26,9 @@ and the CPU baselines.  ``steps`` is the number of split reductions actually tim
   ||Q^T Q - I||_F, ||Z^T Z - I||_F of the last split step (FP64 GEMMs on the device).
 * ``e2e``: one split reduction through the public host entry point paraht_reduce_host with
   pinned host buffers, host<->device copies inside the timed region.
-* ``roofline``: the dominant kernel (the split-precision compact-WY op-list kernel of stage 2),
-  every launch timed with CUDA events on its stream during the timed steps.
+* ``roofline``: the dominant kernel (the split-precision op-list kernel of stage 2), every launch
+  timed with CUDA events on its stream during the timed steps; ``traffic`` is its DRAM bytes per
+  launch from an ncu capture of the same kernel at n=6000, scaled by the flops per launch.
 * ``cpu_baseline``: the CPU oracle (a restatement of the reference's OpenMP algorithm) on a
   bounded sample, scaled by (n / n_sample)^3 to the metric's unit.
 * ``--impl reference``: times that CPU implementation on the host cores (the reference itself
@@ -57,6 +58,11 @@ METRIC = "HT-reduction sec at n=16000: split-prec vs FP64 GPU at bwd err<=1e-13"
 EPS = float(np.finfo(np.float64).eps)
 # FP64 roof when it cannot be measured in the run: 2 FMA/clk/SM x 152 SMs x 2.07 GHz on GB300
 FP64_PEAK_TFLOPS = 1.26
+
+
+# DRAM bytes per FP64-equivalent flop of the split op-list kernel, measured with ncu on the Q and Z
+# lists of one n=6000 sweep group (207.9456 MB over 2.1504 GFLOP)
+TRAFFIC_BYTES_PER_FLOP = 207.9456e6 / 2.1504e9
 
 
 def measure_fp64_peak(torch, n: int = 8192, reps: int = 3):
@@ -727,8 +733,20 @@ def run_pencil(args, rank: int, world: int, local: int):
         measured = "bf16_tflops" in peaks
         peak = float(peaks["bf16_tflops"]) if measured else 1900.0
         achieved = 43.0 * fp64eq if fp64eq else None
+        # DRAM bytes per launch: the ncu capture of the Q and Z lists at n=6000 (207.9 MB of DRAM
+        # reads + writes per 2.1504 GFLOP FP64-equivalent) scaled to this run's mean launch; a list's
+        # bytes and flops both grow as the rows x columns of its span (ops 32 wide, 2048 flops per
+        # strip row per op in either stage-2 variant)
+        per_launch_flops = s2["flops"] / s2["launches"] if s2["launches"] else 0.0
+        traffic = TRAFFIC_BYTES_PER_FLOP * per_launch_flops if per_launch_flops else None
         roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                    "frac": achieved / peak if achieved else None, "traffic": None,
+                    "frac": achieved / peak if achieved else None, "traffic": traffic,
+                    "traffic_unit": "bytes per launch",
+                    "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the Q and Z lists at "
+                                       "n=6000 (0.0967 B per FP64-equivalent flop), scaled by this run's mean "
+                                       "flops per launch; writes still dirty in L2 at kernel end are not counted "
+                                       "(0.125 B/flop with them, the algorithmic figure)"),
+                    "algorithmic_bytes": 0.125 * per_launch_flops if per_launch_flops else None,
                     "kernel": ("k_ws_apply<GeoS2G> (split-precision op lists of the Givens stage 2: dense "
                                "(r+nq)^2 blocks, FP16 digit MMAs)" if args.stage2 == "givens" else
                                "k_ws_apply<GeoS2> (split-precision compact-WY op lists, FP16 digit MMAs)"),

@@ -130,10 +130,7 @@ int check_finite(cudaStream_t s, int n, const double* A, int lda, const double* 
 void dgemm(cudaStream_t s, bool tx, int M, int N, int K, const double* X, int ldx, const double* Y, int ldy,
            double* Out, int ldo);
 void set_identity(cudaStream_t s, int n, double* X, int ldx);
-// Raises a kernel's dynamic shared-memory limit on the current device to at least `bytes`
-// (PARAHT_ERR_CUDA when refused).  The limit is one value per kernel and device, shared by every
-// context, thread and captured graph, so it only ever grows: a call with smaller tiles never takes
-// away the room another call's launch in flight was shaped for.
+// smem_at_least (declared in paraht_internal.cuh): dynamic shared-memory limits only ever grow.
 int smem_at_least(const void* func, size_t bytes);
 // Batched reduction (batched.cu): which pencils the persistent kernel takes, and one launch
 // over the pencils idx[] of the batch on stream s.

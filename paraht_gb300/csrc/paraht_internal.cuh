@@ -15,11 +15,30 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #define PHT_DEV __device__ __forceinline__
 
 namespace pht {
 
 constexpr int kWarp = 32;
+
+// Raises a kernel's dynamic shared-memory limit on the current device to at least `bytes`
+// (PARAHT_ERR_CUDA when refused).  The limit is one value per kernel and device, shared by every
+// context, thread and captured graph, so it only ever grows: a call with smaller tiles never takes
+// away the room another call's launch in flight was shaped for.  (api.cu)
+int smem_at_least(const void* func, size_t bytes);
+
+// The same for a kernel whose shared memory is fixed, on launch paths: after the first grant on a
+// device (bit d of `done`) it costs one cudaGetDevice.  A refusal leaves the bit clear; the launch
+// that follows then fails and its error reaches the caller through the stream checks.
+inline void smem_once(const void* func, size_t bytes, std::atomic<unsigned long long>& done) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (done.load(std::memory_order_acquire) & bit) return;
+  if (smem_at_least(func, bytes) == 0) done.fetch_or(bit, std::memory_order_acq_rel);
+}
 
 // ---------------------------------------------------------------------------------------
 // CTA-wide sum of one double per thread; every thread receives the total.

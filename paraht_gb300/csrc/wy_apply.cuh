@@ -217,11 +217,8 @@ constexpr size_t right_smem() { return sizeof(double) * (size_t)(kRightCCH + kMa
 template <class Geo>
 inline void launch_apply_left(double* X, int ldx, int col0, int col1, const Geo& g, cudaStream_t s) {
   if (col1 < col0) return;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_apply_left<Geo>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kLeftSmem);
-    attr = true;
-  }
+  static std::atomic<unsigned long long> done{0};
+  smem_once((const void*)k_apply_left<Geo>, kLeftSmem, done);
   const int nblk = (col1 - col0 + 1 + kLeftCS - 1) / kLeftCS;
   count_launch();
   KernelClock* kc = tl_kclock;
@@ -235,11 +232,8 @@ inline void launch_apply_left(double* X, int ldx, int col0, int col1, const Geo&
 template <class Geo, int RS = 64>
 inline void launch_apply_right(double* X, int ldx, int row0, int row1, const Geo& g, cudaStream_t s) {
   if (row1 < row0) return;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_apply_right<Geo, RS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)right_smem<RS>());
-    attr = true;
-  }
+  static std::atomic<unsigned long long> done{0};
+  smem_once((const void*)k_apply_right<Geo, RS>, right_smem<RS>(), done);
   const int nblk = (row1 - row0 + 1 + RS - 1) / RS;
   count_launch();
   KernelClock* kc = tl_kclock;

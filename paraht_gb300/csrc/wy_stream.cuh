@@ -790,11 +790,8 @@ inline bool ws_fits(int k_max, int len_max) { return k_max <= kWsK && len_max <=
 // applies it to strip rows [row0, row1] of C viewed with strides (rs, cs).
 template <class Geo, bool kOne>
 inline void ws_set_smem_attr() {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_ws_apply<Geo, kOne>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ws_smem_bytes<kOne>());
-    attr = true;
-  }
+  static std::atomic<unsigned long long> done{0};
+  smem_once((const void*)k_ws_apply<Geo, kOne>, ws_smem_bytes<kOne>(), done);
 }
 
 template <class Geo>
