@@ -412,7 +412,8 @@ int s1_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
     if (const int rc = smem_at_least((const void*)k_s1_right_gen, rsm)) return rc;
 
   // split-precision bulk updates (split_apply.cuh) where the op shapes fit; one operand region
-  // per launch site: 0 B left, 1 A left, 2 Q, 3 remaining B rows, 4 A right, 5 Z right
+  // per launch site: 0 B left, 1 A left, 2 Q, 3 remaining B rows, 4 A and Z right (one list), 5
+  // unused
   const bool sp = ctx.split && split_fits(nb, L);
   void* reg[6] = {};
   if (sp)
@@ -421,7 +422,7 @@ int s1_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
       if (!reg[i]) return PARAHT_ERR_ALLOC;
     }
   cudaEvent_t evL = ctx.ev[0], evAL = ctx.ev[1], evLA = ctx.ev[2], evRest = ctx.ev[3], evChain = ctx.ev[4];
-  cudaEvent_t evZ[2] = {ctx.ev[5], ctx.ev[6]};
+  cudaEvent_t evZ[2] = {ctx.ev[5], ctx.ev[6]}, evPrep = ctx.ev[7];
   if (!serial) {  // side streams start after everything already queued on sA
     cudaEventRecord(evL, sA);
     cudaStreamWaitEvent(sB, evL, 0);
@@ -495,8 +496,20 @@ int s1_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
       cudaStreamWaitEvent(sC, evChain, 0);
       cudaStreamWaitEvent(sA, evAL, 0);  // left update of A done before its right update
     }
-    apply_right_any(reg[4], A, lda, 0, n - 1, GeoS1Right{P, VRc[s], TR[s], -1}, P.nblocks, sA);
-    apply_right_any(reg[5], Z, ldz, 0, n - 1, GeoS1Right{P, VRc[s], TR[s], -1}, P.nblocks, sC);
+    // the panel's right reflectors on A and Z (ab2rht.f90:387-467), one prepared list.  The next
+    // panel's left generation reads A's rows >= jb0 + 2nb only: those rows stay on the chain, the
+    // rows above join the Z update on sC (whose next A left update the next panel's A right
+    // update waits for through evAL)
+    const GeoS1Right gall{P, VRc[s], TR[s], -1};
+    const int split_row = std::min(n, jb0 + 2 * nb);
+    prepare_any(reg[4], gall, P.nblocks, sA);
+    if (!serial) {
+      cudaEventRecord(evPrep, sA);
+      cudaStreamWaitEvent(sC, evPrep, 0);
+    }
+    apply_right_any(reg[4], A, lda, split_row, n - 1, gall, P.nblocks, sA, false);
+    apply_right_any(reg[4], A, lda, 0, split_row - 1, gall, P.nblocks, sC, false);
+    apply_right_any(reg[4], Z, ldz, 0, n - 1, gall, P.nblocks, sC, false);
     if (!serial) cudaEventRecord(evZ[s], sC);
   }
   if (!serial) {  // join

@@ -42,6 +42,7 @@ struct GeoS1Left {
   PHT_DEV bool masks_y() const { return false; }
   // every op applies all its reflectors to every row; one product C -= C M when spans are <= 32
   __host__ __device__ bool one_product_only() const { return P.L <= 32; }
+  __host__ __device__ bool wide_dense() const { return false; }
   PHT_DEV void range(int, const WYOp& w, int, int& a, int& b) const {
     a = 0;
     b = w.k - 1;
@@ -73,6 +74,7 @@ struct GeoS1Q {
   PHT_DEV bool masks_y() const { return false; }
   // every op applies all its reflectors to every row; one product C -= C M when spans are <= 32
   __host__ __device__ bool one_product_only() const { return P.L <= 32; }
+  __host__ __device__ bool wide_dense() const { return false; }
   PHT_DEV void range(int, const WYOp& w, int, int& a, int& b) const {
     a = 0;
     b = w.k - 1;
@@ -107,6 +109,7 @@ struct GeoS1Right {
   PHT_DEV bool masks_y() const { return false; }
   // every op applies all its reflectors to every row; one product C -= C M when spans are <= 32
   __host__ __device__ bool one_product_only() const { return P.L <= 32; }
+  __host__ __device__ bool wide_dense() const { return false; }
   PHT_DEV void range(int, const WYOp& w, int, int& a, int& b) const {
     a = 0;
     b = w.k - 1;

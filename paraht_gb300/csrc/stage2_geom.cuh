@@ -38,6 +38,7 @@ struct GeoS2 {
     const bool full = kind == kUpQ || kind == kUpZ || kind == kUpLeft || kind == kLaLeftA || kind == kLaLeftB;
     return full && r + nq <= 32;
   }
+  __host__ __device__ bool wide_dense() const { return false; }
   static constexpr int kSite = 1;  // stage-2 op list (kernel statistics)
   // Reflectors [a, b] (0-based) of op o applied to strip row `row` (0-based, lo <= row <= hi).
   PHT_DEV void range(int o, const WYOp& w, int row, int& a, int& b) const {

@@ -174,9 +174,9 @@ int s2g_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, 
     cudaEventRecord(ctx.ev_a, sg);
     cudaStreamWaitEvent(su, ctx.ev_a, 0);
   }
-  // split-precision dense ops (one-product form) when r + nq <= 32; operand regions: 0 bulk
+  // split-precision dense ops (one-product forms) when r + nq <= 48; operand regions: 0 bulk
   // right, 1 bulk left (both shared by A and B), 2 Q, 3 Z, 4 lookahead left B, 5 lookahead left A
-  const bool sp = ctx.split && r + nq <= kWsMM;
+  const bool sp = ctx.split && r + nq <= kWsMW;
   void* reg[6] = {};
   if (sp)
     for (int i = 0; i < 6; ++i) {

@@ -92,8 +92,10 @@ struct GeoS2G {
   PHT_DEV int op_slot(int o) const { return o; }
   static constexpr int kSite = 1;  // stage-2 op list (kernel statistics)
   PHT_DEV bool masks_y() const { return false; }
-  // every op is a full product C -= C (I - G); the split kernel's one-product form when it fits
+  // every op is a full product C -= C (I - G): the split kernel's one-product form when it fits
+  // 32 columns, its wide dense form up to 48
   __host__ __device__ bool one_product_only() const { return r + nq <= 32; }
+  __host__ __device__ bool wide_dense() const { return r + nq > 32; }
   PHT_DEV void range(int, const WYOp& w, int, int& a, int& b) const {
     a = 0;
     b = w.k - 1;

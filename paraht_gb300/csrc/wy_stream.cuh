@@ -37,7 +37,12 @@
 // Y vanishes before a), and the two-product form applies; Geo::masks_y selects the three-product
 // form.
 //
-// Limits: k <= 16 reflectors, span len <= 64 per op.
+// One-product forms.  Lists whose ops all apply every reflector to every row take C -= C M with
+// M = V T V^T (formed once per op, span <= 32); the dense ops of the Givens stage 2 (V = I,
+// M = I - G, an accumulated block of rotations) take the same form, up to 48 wide in lists of
+// their own (WsOpMW operands; the level sums are taken out after 32 inner terms).
+//
+// Limits: k <= 16 reflectors, span len <= 64 per op; dense ops len <= 48.
 #pragma once
 #include <cuda_fp16.h>
 #include <stddef.h>
@@ -62,6 +67,8 @@ constexpr int kWsPL = kWsLen + 8;  // fp16 pitch of len-indexed digit rows (conf
 constexpr int kWsPK = kWsK + 8;    // fp16 pitch of k-indexed digit rows
 constexpr int kWsMM = 32;          // largest span with the one-product form C -= C M
 constexpr int kWsPM = kWsMM + 8;   // fp16 pitch of M's digit rows
+constexpr int kWsMW = 48;          // largest dense op of the wide one-product form
+constexpr int kWsPMW = kWsMW + 8;  // fp16 pitch of its digit rows
 constexpr int kWsHead = 5;         // headroom bits of the row scale at load time
 constexpr int kWsGuard = 57;       // a row is shifted down before an op when a value passes 2^57
 constexpr int kWsNoScale = -2000;  // row scale not set yet (no nonzero value loaded)
@@ -80,6 +87,15 @@ struct WsOpDigits {
   int ft[kWsK];                           // scale of column m of T
   int fvt[kWsLen];                        // scale of row c of V
 };
+
+// Operands of a dense op of a wide list (Geo::wide_dense(): every op dense, len <= kWsMW), written
+// over the op's WsOpDigits slot.
+struct WsOpMW {
+  uint16_t mt[kWsD][kWsMW][kWsPMW];  // M [c_out][c_in]
+  int fm[kWsMW];                     // scale of column c_out of M
+};
+static_assert(sizeof(WsOpMW) <= sizeof(WsOpDigits), "a wide op fits its slot");
+static_assert(sizeof(WsOpMW) % 16 == 0, "copied in 16-byte words");
 
 // ------------------------------------------------------------------------------------------
 // Integer helpers (no FP64 pipe)
@@ -199,7 +215,7 @@ __global__ void __launch_bounds__(128) k_ws_prep(Geo g, WsOpDigits* out) {
   __shared__ double Vs[kWsLen][kWsK + 1];  // V[c][m]
   __shared__ double Tsh[kWsK][kWsK + 1];   // T[l][m]
   __shared__ double Wsh[kWsK][kWsLen + 1]; // W[m][c] (two-product form)
-  __shared__ double Msh[kWsMM][kWsMM + 1]; // M[c_in][c_out] = V W (one-product form)
+  __shared__ double Msh[kWsMW][kWsMW + 1]; // M[c_in][c_out] = V W (one-product forms)
   __shared__ int sc[kWsLen];
   __shared__ int scv[kWsK];  // V's column scales (sc is reused for M's and W's columns)
   const int slot = blockIdx.x;
@@ -210,27 +226,33 @@ __global__ void __launch_bounds__(128) k_ws_prep(Geo g, WsOpDigits* out) {
   const int len = live ? op.len : 0, k = live ? op.k : 0;
   const bool two = !g.masks_y();
   if (op.dense) {
-    // C -= C M with M = T = I - G given explicitly (len <= kWsMM, one-product form only)
-    for (int e = t; e < kWsMM * kWsMM; e += 128) {
-      const int ci = e % kWsMM, co = e / kWsMM;
+    // C -= C M with M = T = I - G given explicitly (one-product forms only): width kWsMM, or
+    // kWsMW in the WsOpMW layout for a wide list
+    const bool wide = g.wide_dense();
+    const int mw = wide ? kWsMW : kWsMM, pm = wide ? kWsPMW : kWsPM;
+    uint16_t* mt = wide ? &reinterpret_cast<WsOpMW*>(D)->mt[0][0][0] : &D->mt[0][0][0];
+    int* fm = wide ? reinterpret_cast<WsOpMW*>(D)->fm : D->fm;
+    for (int e = t; e < mw * mw; e += 128) {
+      const int ci = e % mw, co = e / mw;
       Msh[ci][co] = (ci < len && co < len) ? op.T[ci + (size_t)co * op.ldt] : 0.0;
     }
     __syncthreads();
-    {  // scales of M's columns: 4 lanes per column
-      const int co = t >> 2, part = t & 3;
+    for (int co0 = 0; co0 < mw; co0 += 32) {  // scales of M's columns: 4 lanes per column
+      const int co = co0 + (t >> 2), part = t & 3;
       uint64_t amax = 0;
-      for (int c = part; c < kWsMM; c += 4) amax = max(amax, ws_abs_bits(Msh[c][co]));
+      if (co < mw)
+        for (int c = part; c < mw; c += 4) amax = max(amax, ws_abs_bits(Msh[c][co]));
       amax = max(amax, (uint64_t)__shfl_xor_sync(0xffffffffu, (long long)amax, 1));
       amax = max(amax, (uint64_t)__shfl_xor_sync(0xffffffffu, (long long)amax, 2));
-      if (part == 0) {
-        D->fm[co] = ws_exp_bits(amax);
+      if (part == 0 && co < mw) {
+        fm[co] = ws_exp_bits(amax);
         sc[co] = ws_exp_bits(amax);
       }
     }
     __syncthreads();
-    for (int e = t; e < kWsMM * kWsPM; e += 128) {
-      const int co = e / kWsPM, ci2 = e % kWsPM;
-      ws_put_digits(&D->mt[0][co][ci2], kWsMM * kWsPM, ci2 < kWsMM ? Msh[ci2][co] : 0.0, sc[co]);
+    for (int e = t; e < mw * pm; e += 128) {
+      const int co = e / pm, ci2 = e % pm;
+      ws_put_digits(mt + (size_t)co * pm + ci2, mw * pm, ci2 < mw ? Msh[ci2][co] : 0.0, sc[co]);
     }
     return;
   }
@@ -354,11 +376,14 @@ struct WsOpM {
   int fm[kWsMM];
 };
 static_assert(sizeof(WsOpM) == offsetof(WsOpDigits, vd), "WsOpM is the prefix of WsOpDigits");
-// kOne: every op of the list takes the one-product form (full reflector ranges, len <= kWsMM),
-// so only M's digits are staged: 57 KB instead of 104 KB, three CTAs per SM.
-template <bool kOne>
+// List forms: 0 general (each op in the one-, two- or three-product form it allows); 1 every op
+// takes the one-product form (full reflector ranges, len <= kWsMM), so only M's digits are
+// staged: 57 KB instead of 104 KB, three CTAs per SM; 2 every op is a dense op of a wide list
+// (len <= kWsMW, WsOpMW operands): 80 KB, two CTAs per SM.
+template <int kForm>
 struct WsSmemT {
-  typename std::conditional<kOne, WsOpM, WsOpDigits>::type op;  // the current op's operand digits
+  typename std::conditional<kForm == 0, WsOpDigits,
+                            typename std::conditional<kForm == 1, WsOpM, WsOpMW>::type>::type op;  // the current op
   long long win[kWsRows][kWsCW + 1];           // resident values (fixed point)
   unsigned long long dirty[kWsRows];           // slots modified since loaded (one bit per slot)
   int escale[kWsRows];                         // row scales
@@ -366,8 +391,8 @@ struct WsSmemT {
 };
 static_assert(kWsCW == 64, "dirty masks hold one bit per slot");
 
-template <bool kOne>
-inline size_t ws_smem_bytes() { return sizeof(WsSmemT<kOne>); }
+template <int kForm>
+inline size_t ws_smem_bytes() { return sizeof(WsSmemT<kForm>); }
 
 // round(a 2^s), a < 2^62, 64-bit only
 PHT_DEV uint64_t ws_scale64(uint64_t a, int s) {
@@ -458,12 +483,13 @@ PHT_DEV void ws_to_afrag(__int128 (*xs)[2][2], const int (*xe)[2][2], int* emax,
   ws_afrag(F, neg, af);
 }
 
-template <class Geo, bool kOne>
-__global__ void __launch_bounds__(kWsThreads, kOne ? 3 : 2)
+template <class Geo, int kForm>
+__global__ void __launch_bounds__(kWsThreads, kForm == 1 ? 3 : 2)
     k_ws_apply(double* __restrict__ C, long long rs, long long cs, int row0, int row1, Geo g,
                const WsOpDigits* __restrict__ prep, unsigned long long* __restrict__ flops) {
   extern __shared__ __align__(16) unsigned char ws_raw[];
-  WsSmemT<kOne>& S = *reinterpret_cast<WsSmemT<kOne>*>(ws_raw);
+  constexpr bool kOne = kForm != 0;  // every op of the list is one product C -= C M
+  WsSmemT<kForm>& S = *reinterpret_cast<WsSmemT<kForm>*>(ws_raw);
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const int gq = lane >> 2, tq = lane & 3;
   const int rbeg = row0 + blockIdx.x * kWsRows;
@@ -503,7 +529,7 @@ __global__ void __launch_bounds__(kWsThreads, kOne ? 3 : 2)
     const int need_rest = kOne ? 0 : __syncthreads_or(wact && !wone);
     if (kOne) __syncthreads();
     {
-      const size_t bytes = need_rest ? sizeof(WsOpDigits) : offsetof(WsOpDigits, vd);
+      const size_t bytes = kForm == 2 ? sizeof(WsOpMW) : need_rest ? sizeof(WsOpDigits) : offsetof(WsOpDigits, vd);
       const uint4* src = reinterpret_cast<const uint4*>(prep + g.op_slot(o));
       uint4* dst = reinterpret_cast<uint4*>(&S.op);
       for (int e = t; e < (int)(bytes / 16); e += kWsThreads) dst[e] = src[e];
@@ -680,6 +706,73 @@ __global__ void __launch_bounds__(kWsThreads, kOne ? 3 : 2)
           }
       }
     };
+    if constexpr (kForm == 2) {
+      // ---- wide dense op, C -= C M with len <= 48: three k-steps.  The FP32 level sums are exact
+      // for at most 32 terms, so the first two k-steps' levels are taken out before the third;
+      // C's third k-step fragments are rebuilt per 16-column group from columns 32..47, which
+      // only the last group's correction (after its products) modifies ----
+      uint32_t af0[kWsD][4], af1[kWsD][4];
+      cfrag(0, af0);
+      if (lenp > 16) cfrag(16, af1);
+      const bool act0 = on0 && erow0 != kWsNoScale, act1 = on1 && erow1 != kWsNoScale;
+      for (int c0 = 0; c0 < lenp; c0 += 16) {
+        long long nh[2][2][2], nl[2][2][2];  // [hh][nt][j]
+        {
+          float acc[kWsLv][2][4];
+          ws_zero_acc(acc);
+          ws_mma_step<kWsPMW>(acc, af0, &S.op.mt[0][0][0], kWsMW * kWsPMW, c0, 0, gq, tq);
+          if (lenp > 16) ws_mma_step<kWsPMW>(acc, af1, &S.op.mt[0][0][0], kWsMW * kWsPMW, c0, 16, gq, tq);
+#pragma unroll
+          for (int hh = 0; hh < 2; ++hh)
+#pragma unroll
+            for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+              for (int j = 0; j < 2; ++j) {
+                nh[hh][nt][j] = nl[hh][nt][j] = 0;
+                ws_levels_of(acc, hh, nt, j, nh[hh][nt][j], nl[hh][nt][j]);
+              }
+        }
+        if (lenp > 32) {
+          uint32_t af2[kWsD][4];
+          cfrag(32, af2);
+          float acc[kWsLv][2][4];
+          ws_zero_acc(acc);
+          ws_mma_step<kWsPMW>(acc, af2, &S.op.mt[0][0][0], kWsMW * kWsPMW, c0, 32, gq, tq);
+#pragma unroll
+          for (int hh = 0; hh < 2; ++hh)
+#pragma unroll
+            for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+              for (int j = 0; j < 2; ++j) ws_levels_of(acc, hh, nt, j, nh[hh][nt][j], nl[hh][nt][j]);
+        }
+        // C -= the summed levels, as in correct() with the right factor's column scales fm
+        const int zrow[2] = {erow0, erow1};
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh) {
+          if (!(hh ? act1 : act0)) continue;
+          const int rr = hh ? rB : rA;
+          const int er = hh ? efix1 : efix0, zr = zrow[hh];
+#pragma unroll
+          for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+              const int cc = c0 + nt * 8 + 2 * tq + j;
+              if (cc >= len) continue;
+              const int fc = S.op.fm[cc];
+              if (fc == kWsNoScale) continue;
+              const long long h = nh[hh][nt][j], l = nl[hh][nt][j];
+              if ((h | l) == 0) continue;
+              const int sh = zr + fc - 8 - er;
+              const long long ah = h < 0 ? -h : h, al = l < 0 ? -l : l;
+              const long long dh = (long long)ws_scale64((uint64_t)ah, sh + 35);
+              const long long dl = (long long)ws_scale64((uint64_t)al, sh);
+              S.win[rr][(op.start + cc) & (kWsCW - 1)] -= (h < 0 ? -dh : dh) + (l < 0 ? -dl : dl);
+            }
+        }
+      }
+      __syncwarp();
+      continue;
+    }
     if (wone) {
       // ---- one product: C -= C M (len <= 32: two k-steps, two 16-column groups) ----
       uint32_t af0[kWsD][4], af1[kWsD][4];
@@ -788,21 +881,23 @@ inline bool ws_fits(int k_max, int len_max) { return k_max <= kWsK && len_max <=
 
 // Prepares the op list (nslots prep slots, Geo::slot_op; skipped when prepare is false) and
 // applies it to strip rows [row0, row1] of C viewed with strides (rs, cs).
-template <class Geo, bool kOne>
+template <class Geo, int kForm>
 inline void ws_set_smem_attr() {
   static std::atomic<unsigned long long> done{0};
-  smem_once((const void*)k_ws_apply<Geo, kOne>, ws_smem_bytes<kOne>(), done);
+  smem_once((const void*)k_ws_apply<Geo, kForm>, ws_smem_bytes<kForm>(), done);
 }
 
 template <class Geo>
 inline void launch_ws_apply(double* C, long long rs, long long cs, int row0, int row1, const Geo& g, int nslots,
                             WsOpDigits* prep, cudaStream_t s, bool prepare = true) {
   if (row1 < row0 || nslots <= 0) return;
-  const bool one = g.one_product_only();
-  if (one)
-    ws_set_smem_attr<Geo, true>();
+  const int form = g.wide_dense() ? 2 : g.one_product_only() ? 1 : 0;
+  if (form == 2)
+    ws_set_smem_attr<Geo, 2>();
+  else if (form == 1)
+    ws_set_smem_attr<Geo, 1>();
   else
-    ws_set_smem_attr<Geo, false>();
+    ws_set_smem_attr<Geo, 0>();
   if (prepare) {
     count_launch();
     k_ws_prep<Geo><<<nslots, 128, 0, s>>>(g, prep);
@@ -814,10 +909,12 @@ inline void launch_ws_apply(double* C, long long rs, long long cs, int row0, int
   const bool timed = kc && kc->pair(Geo::kSite, &e0, &e1);
   if (timed) cudaEventRecord(e0, s);
   unsigned long long* fl = timed ? kc->dflops + Geo::kSite : nullptr;
-  if (one)
-    k_ws_apply<Geo, true><<<nblk, kWsThreads, ws_smem_bytes<true>(), s>>>(C, rs, cs, row0, row1, g, prep, fl);
+  if (form == 2)
+    k_ws_apply<Geo, 2><<<nblk, kWsThreads, ws_smem_bytes<2>(), s>>>(C, rs, cs, row0, row1, g, prep, fl);
+  else if (form == 1)
+    k_ws_apply<Geo, 1><<<nblk, kWsThreads, ws_smem_bytes<1>(), s>>>(C, rs, cs, row0, row1, g, prep, fl);
   else
-    k_ws_apply<Geo, false><<<nblk, kWsThreads, ws_smem_bytes<false>(), s>>>(C, rs, cs, row0, row1, g, prep, fl);
+    k_ws_apply<Geo, 0><<<nblk, kWsThreads, ws_smem_bytes<0>(), s>>>(C, rs, cs, row0, row1, g, prep, fl);
   if (timed) cudaEventRecord(e1, s);
 }
 

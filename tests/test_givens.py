@@ -68,7 +68,8 @@ def test_givens_pipelined_bitwise_equals_sequential(ctx, oracle, n, r, nq):
         assert np.array_equal(X, Y)
 
 
-@pytest.mark.parametrize("n,r,p,nq,dist", [(400, 16, 4, 16, "std"), (300, 16, 3, 8, "graded"), (257, 8, 4, 8, "refcompat")])
+@pytest.mark.parametrize("n,r,p,nq,dist", [(400, 16, 4, 16, "std"), (300, 16, 3, 8, "graded"), (257, 8, 4, 8, "refcompat"),
+                                           (420, 32, 4, 16, "std"), (380, 24, 3, 24, "graded")])
 def test_givens_reduce_end_to_end(oracle, ctx, n, r, p, nq, dist):
     A0, B0 = make(n, dist)
     for flags, tol in ((ph.PARAHT_FLAG_GIVENS, 10 * n * EPS), (ph.PARAHT_FLAG_GIVENS | ph.PARAHT_FLAG_SPLIT, 1e-13)):
@@ -83,10 +84,16 @@ def test_givens_reduce_end_to_end(oracle, ctx, n, r, p, nq, dist):
             assert abs_rel_max_diff(A, Ah) < 1e-8 and abs_rel_max_diff(B, np.triu(Bh)) < 1e-8
 
 
-def test_givens_split_matches_fp64(ctx, oracle):
-    """The split-precision dense ops (one-product form) against the FP64 dense ops, same input."""
+@pytest.mark.parametrize("n,r,nq", [
+    (300, 16, 16),  # dense ops 32 wide: the one-product form
+    (301, 24, 8),   # 32 wide, ragged last block
+    (300, 32, 16),  # 48 wide: the wide dense form
+    (317, 24, 24),  # 48 wide, ragged
+    (290, 20, 20),  # 40 wide: three k-steps, the last one partly empty
+])
+def test_givens_split_matches_fp64(ctx, oracle, n, r, nq):
+    """The split-precision dense ops (one-product forms) against the FP64 dense ops, same input."""
     torch = pytest.importorskip("torch")
-    n, r, nq = 300, 16, 16
     A0, B0 = make(n)
     S1 = oracle_reduce(oracle, A0, B0, r, 4, nq, stage=1)
     f = _dev_rht2ht(torch, ctx, copies(*S1), r, nq, ph.PARAHT_FLAG_GIVENS)
