@@ -209,6 +209,11 @@ int paraht_gghd3(char compq, char compz, int n, int ilo, int ihi, double* A, int
  * reported: PARAHT_ERR_TIMEOUT when the wait gave up as designed (the context stays usable),
  * 0 if it did not, PARAHT_ERR_CUDA on a launch failure, -2 for an invalid spin_limit. */
 int paraht_selftest_wait_timeout(paraht_ctx ctx, long long spin_limit);
+/* Self-test of the branch-free reflector scalars the generation chains use (DLARFG's tau, scal =
+ * 1/(alpha - beta), beta from alpha and the squared norm of the reflector's tail): for i < count,
+ * out[3i..3i+2] = tau, scal, beta of (alpha[i], xnorm2[i]); device pointers, stream-ordered on the
+ * context's stream and synchronised.  -2 for count < 0, -3 for a null pointer. */
+int paraht_selftest_reflector(paraht_ctx ctx, int count, const double* alpha, const double* xnorm2, double* out);
 
 /* ---- misc ---- */
 const char* paraht_strerror(int status);

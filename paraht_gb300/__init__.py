@@ -194,6 +194,11 @@ class Context:
         (PARAHT_ERR_TIMEOUT, -1003, when the failure path works)."""
         return int(lib().paraht_selftest_wait_timeout(self._h, int(spin_limit)))
 
+    def selftest_reflector(self, count: int, alpha_ptr: int, xnorm2_ptr: int, out_ptr: int) -> None:
+        """Reflector scalars (tau, scal, beta per entry) of the generation chains' branch-free
+        formula for device arrays alpha, xnorm2 (paraht_selftest_reflector)."""
+        check(lib().paraht_selftest_reflector(self._h, int(count), alpha_ptr, xnorm2_ptr, out_ptr), "selftest_reflector")
+
     def phase_times(self) -> dict:
         buf = (C.c_double * 8)()
         check(lib().paraht_ctx_phase_times(self._h, buf, 8), "phase_times")

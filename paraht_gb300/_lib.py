@@ -63,6 +63,7 @@ SIGNATURES = {
     "paraht_gghd3": [C.c_char, C.c_char, _i, _i, _i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i, _i, _i],
     "paraht_gghd3_d": [C.c_void_p, C.c_char, C.c_char, _i, _i, _i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i, _i, _i],
     "paraht_selftest_wait_timeout": [C.c_void_p, C.c_longlong],
+    "paraht_selftest_reflector": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p],
     "paraht_strerror": [_i],
     "paraht_version": [],
 }

@@ -933,6 +933,25 @@ extern "C" int paraht_selftest_wait_timeout(paraht_ctx c, long long spin_limit) 
   return rc;
 }
 
+namespace pht {
+void launch_reflector_selftest(cudaStream_t s, int count, const double* alpha, const double* xnorm2, double* out);
+}
+
+extern "C" int paraht_selftest_reflector(paraht_ctx c, int count, const double* alpha, const double* xnorm2,
+                                         double* out) {
+  if (!ctx_ok(c)) return PARAHT_ERR_BAD_CTX;
+  if (count < 0) return -2;
+  if (count > 0 && (!alpha || !xnorm2 || !out)) return -3;
+  Ctx& x = c->c;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(x.device);
+  pht::launch_reflector_selftest(x.stream, count, alpha, xnorm2, out);
+  const int rc = finish(x);
+  cudaSetDevice(prev);
+  return rc;
+}
+
 // ---- DGGHD3-compatible entry ----
 static int gghd3_check(char compq, char compz, int n, int ilo, int ihi, const double* A, int lda, const double* B,
                        int ldb, const double* Q, int ldq, const double* Z, int ldz, int r, int p, int nq) {

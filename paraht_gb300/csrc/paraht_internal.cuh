@@ -94,6 +94,43 @@ PHT_DEV Reflector make_reflector(double alpha, double xnorm2) {
   return h;
 }
 
+// The same scalars without branches, for the latency-bound factorisation chains: the reciprocal
+// square root and the reciprocal come from the hardware approximations (PTX rsqrt.approx.ftz.f64,
+// rcp.approx.ftz.f64) refined by two Newton-Raphson steps each (y += y (1 - x y^2) / 2 and
+// y += y (1 - x y); each step doubles the correct bits), so the compiler can interleave them
+// with independent work (a shuffle reduction) instead of branching into library code.  Within a
+// few ulps of make_reflector's values; tau = 0, scal = 1, beta = alpha when xnorm2 == 0.
+PHT_DEV double rsqrt_seed(double x) {
+  double y;
+  asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  return y;
+}
+PHT_DEV double rcp_seed(double x) {
+  double y;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  return y;
+}
+PHT_DEV Reflector make_reflector_nr(double alpha, double xnorm2) {
+  const double s = fma(alpha, alpha, xnorm2);
+  double rho = rsqrt_seed(s);
+#pragma unroll
+  for (int it = 0; it < 2; ++it) {
+    const double e = fma(-s * rho, rho, 1.0);
+    rho = fma(0.5 * rho, e, rho);
+  }
+  const double nrm = s * rho, aa = fabs(alpha);
+  const double den = aa + nrm;
+  double inv = rcp_seed(den);
+#pragma unroll
+  for (int it = 0; it < 2; ++it) inv = fma(inv, fma(-den, inv, 1.0), inv);
+  const bool zero = xnorm2 == 0.0;
+  Reflector h;
+  h.tau = zero ? 0.0 : fma(aa, rho, 1.0);
+  h.scal = zero ? 1.0 : copysign(inv, alpha);
+  h.beta = zero ? alpha : -copysign(nrm, alpha);
+  return h;
+}
+
 // ---------------------------------------------------------------------------------------
 // Compact-WY op descriptors.
 // ---------------------------------------------------------------------------------------

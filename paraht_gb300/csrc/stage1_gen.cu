@@ -25,6 +25,21 @@ int s1_gen_grant() {
   return smem_at_least((const void*)k_s1_rgen, 227 * 1024);
 }
 
+__global__ void k_reflector_selftest(int count, const double* alpha, const double* xnorm2, double* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const Reflector h = reflector_from_norm2(alpha[i], xnorm2[i]);
+  out[3 * i] = h.tau;
+  out[3 * i + 1] = h.scal;
+  out[3 * i + 2] = h.beta;
+}
+
+void launch_reflector_selftest(cudaStream_t s, int count, const double* alpha, const double* xnorm2, double* out) {
+  if (count <= 0) return;
+  count_launch();
+  k_reflector_selftest<<<(count + 255) / 256, 256, 0, s>>>(count, alpha, xnorm2, out);
+}
+
 void launch_s1_lgen(cudaStream_t s, double* A, int lda, const S1Panel& P, double* VL, double* TL) {
   count_launch();
   k_s1_lgen<<<1, s1_lgen_threads(P.nb), s1_lgen_smem(P.L, P.nb), s>>>(A, lda, P, VL, TL);

@@ -26,9 +26,9 @@ inline __host__ __device__ int s1_round16(int x) { return (x + 15) / 16 * 16; }
 inline __host__ __device__ int s1_lgen_pitch(int L) { return s1_round16(L) + 8; }
 inline __host__ __device__ int s1_rgen_pitch(int L) { return s1_round16(L) + 4; }
 
-// Reflector scalars of DLARFG from alpha and the squared norm of x (see make_reflector).
+// Reflector scalars of DLARFG from alpha and the squared norm of x (see make_reflector_nr):
 // tau, scal = 1/(alpha-beta), beta.
-PHT_DEV Reflector reflector_from_norm2(double alpha, double xnorm2) { return make_reflector(alpha, xnorm2); }
+PHT_DEV Reflector reflector_from_norm2(double alpha, double xnorm2) { return make_reflector_nr(alpha, xnorm2); }
 
 // Sum over groups of G consecutive lanes (G = 4 or 8), result in every lane of the group.
 template <int G>

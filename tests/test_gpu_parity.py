@@ -109,6 +109,35 @@ def test_time_chain_keeps_results_and_adds_up(ctx, flags):
     assert 0.5 * t["total"] < parts <= 1.01 * t["total"]
 
 
+def test_reflector_scalars_newton(ctx):
+    """The generation chains' branch-free reflector scalars (hardware rsqrt/rcp approximations
+    refined by Newton-Raphson steps) against the exact values in extended precision: tau = 1 +
+    |alpha|/nrm, scal = sign(alpha)/(|alpha| + nrm), beta = -sign(alpha) nrm, nrm = sqrt(alpha^2 +
+    xnorm2), each within 4 ulps; tau = 0, scal = 1, beta = alpha when xnorm2 = 0."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(5)
+    m = 100000
+    alpha = rng.standard_normal(m) * 10.0 ** rng.uniform(-100, 100, m)
+    xn2 = (rng.standard_normal(m) * 10.0 ** rng.uniform(-100, 100, m)) ** 2
+    alpha[:50] = 0.0
+    xn2[50:100] = 0.0
+    xn2[100:150] = alpha[100:150] ** 2 * 1e-30  # tail far below alpha
+    alpha[150:200] = alpha[150:200] * 1e-30     # alpha far below the tail
+    da, dx = torch.from_numpy(alpha).cuda(), torch.from_numpy(xn2).cuda()
+    out = torch.empty(3 * m, dtype=torch.float64, device="cuda")
+    ctx.selftest_reflector(m, da.data_ptr(), dx.data_ptr(), out.data_ptr())
+    tau, scal, beta = out.cpu().numpy().reshape(m, 3).T
+    z = xn2 == 0.0
+    assert np.all(tau[z] == 0.0) and np.all(scal[z] == 1.0) and np.array_equal(beta[z], alpha[z])
+    a, x = alpha[~z].astype(np.longdouble), xn2[~z].astype(np.longdouble)
+    nrm = np.sqrt(a * a + x)
+    sg = np.where(np.signbit(alpha[~z]), -1.0, 1.0).astype(np.longdouble)
+    ref = (1 + np.abs(a) / nrm, sg / (np.abs(a) + nrm), -sg * nrm)
+    for got, want in zip((tau[~z], scal[~z], beta[~z]), ref):
+        rel = np.abs((got.astype(np.longdouble) - want) / want)
+        assert float(rel.max()) <= 4 * EPS
+
+
 @pytest.mark.parametrize("n", [1, 2, 3, 4, 6, 9])
 def test_tiny_sizes(oracle, n):
     r, p, nq = 2, 2, 2
