@@ -359,8 +359,8 @@ def run_batch(args, rank: int, world: int, local: int):
             "e2e": {"value": v, "unit": "pencils/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}), flush=True)
         return 0
 
-    # the batched call runs up to 8 worker contexts of 3 streams each beside the persistent
-    # launch: ask for more hardware queues than CUDA's default 8 (read at context creation)
+    # the batched call runs up to 8 worker contexts of 4 streams each beside the persistent
+    # launch: ask for 32 hardware queues instead of CUDA's default 8 (read at context creation)
     os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     import torch
 

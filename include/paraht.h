@@ -158,8 +158,12 @@ int paraht_rht2ht_d_noalloc(paraht_ctx ctx, int n, double* A, int lda, double* B
  * persistent launch, one CTA per pencil at a time, largest first; their results are bitwise
  * those of paraht_reduce_d in FP64 (also when PARAHT_FLAG_SPLIT is set).  The other pencils go
  * through the single-pencil path, largest first, up to eight at a time on internal worker
- * contexts (own streams and workspace), overlapping the persistent launch.
- * PARAHT_FLAG_BATCH_LOOP sends every pencil through paraht_reduce_d (the looped baseline);
+ * contexts (own streams and workspace; their bulk lists on two side streams), overlapping the
+ * persistent launch.  The worker contexts together use 32 streams: run with
+ * CUDA_DEVICE_MAX_CONNECTIONS=32 (set before the process creates its CUDA context), or streams
+ * share hardware queues and the pencils' kernels wait behind one another.
+ * PARAHT_FLAG_BATCH_LOOP reduces the pencils one after the other with paraht_reduce_d on this
+ * context (the looped baseline);
  * PARAHT_FLAG_GIVENS is refused (PARAHT_ERR_NOT_SUPPORTED).
  * Pointers of different pencils must not overlap. ---- */
 #define PARAHT_BATCH_MAX_N 1024

@@ -178,7 +178,17 @@ using pht::Ctx;
 
 static int ctx_ok(paraht_ctx c) { return c && c->magic == kMagic; }
 
-extern "C" int paraht_ctx_create(paraht_ctx* out, int device) {
+// lean: a batched call's worker context, whose stage-2 bulk lists share two side streams (B and Q
+// on one, A and Z on the other) instead of four, so that the worker contexts of a batch together
+// stay within the device's hardware queues (CUDA_DEVICE_MAX_CONNECTIONS, at most 32): streams
+// beyond them share queues, and a chain kernel of one pencil then waits behind another
+// pencil's bulk launch.  The pencils of the batch provide the concurrency the four streams give
+// a lone pencil.
+static int ctx_create(paraht_ctx* out, int device, bool lean);
+
+extern "C" int paraht_ctx_create(paraht_ctx* out, int device) { return ctx_create(out, device, false); }
+
+static int ctx_create(paraht_ctx* out, int device, bool lean) {
   if (!out) return -1;
   *out = nullptr;
   int ndev = 0;
@@ -212,8 +222,14 @@ extern "C" int paraht_ctx_create(paraht_ctx* out, int device) {
     if (!rc && cudaEventCreateWithFlags(&x.ev_enter, cudaEventDisableTiming) != cudaSuccess) rc = PARAHT_ERR_CUDA;
     if (!rc && cudaEventCreateWithFlags(&x.ev_exit, cudaEventDisableTiming) != cudaSuccess) rc = PARAHT_ERR_CUDA;
   }
-  if (!rc && cudaStreamCreateWithFlags(&x.side3, cudaStreamNonBlocking) != cudaSuccess) rc = PARAHT_ERR_CUDA;
-  if (!rc && cudaStreamCreateWithFlags(&x.side4, cudaStreamNonBlocking) != cudaSuccess) rc = PARAHT_ERR_CUDA;
+  if (lean) {
+    x.side3 = x.side;
+    x.side4 = x.side2;
+    x.lean = true;
+  } else {
+    if (!rc && cudaStreamCreateWithFlags(&x.side3, cudaStreamNonBlocking) != cudaSuccess) rc = PARAHT_ERR_CUDA;
+    if (!rc && cudaStreamCreateWithFlags(&x.side4, cudaStreamNonBlocking) != cudaSuccess) rc = PARAHT_ERR_CUDA;
+  }
   for (auto& e : x.ev_s2)
     if (!rc && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) rc = PARAHT_ERR_CUDA;
   for (auto& e : x.ev)
@@ -248,7 +264,7 @@ extern "C" int paraht_ctx_destroy(paraht_ctx c) {
     cudaStreamDestroy(x.side);
   }
   for (cudaStream_t* sp : {&x.side2, &x.side3, &x.side4, &x.crit})
-    if (*sp) {
+    if (*sp && !(x.lean && (sp == &x.side3 || sp == &x.side4))) {  // a lean context's side3/4 alias side/side2
       cudaStreamSynchronize(*sp);
       cudaStreamDestroy(*sp);
     }
@@ -870,7 +886,8 @@ extern "C" int paraht_reduce_batched_d(paraht_ctx c, int count, const int* n, do
   // the other pencils through the single-pencil path, overlapping the persistent launch: several
   // at once on worker contexts (own streams and workspace, one host thread each), since one
   // pencil's serial chains leave most SMs idle
-  const int nworkers = std::min<int>(pht::kBatchWorkers, (int)large.size());
+  // PARAHT_FLAG_BATCH_LOOP: the looped baseline, one paraht_reduce_d after the other on this context
+  const int nworkers = (flags & PARAHT_FLAG_BATCH_LOOP) ? 1 : std::min<int>(pht::kBatchWorkers, (int)large.size());
   if (!rc && nworkers <= 1) {
     for (int i : large) {
       rc = run_device(x, 3, n[i], A[i], lda[i], B[i], ldb[i], Q[i], ldq[i], Z[i], ldz[i], r[i], p[i], nq[i],
@@ -881,7 +898,7 @@ extern "C" int paraht_reduce_batched_d(paraht_ctx c, int count, const int* n, do
   } else if (!rc) {
     while ((int)x.workers.size() < nworkers && !rc) {
       paraht_ctx w = nullptr;
-      rc = paraht_ctx_create(&w, x.device);
+      rc = ctx_create(&w, x.device, true);
       if (!rc) x.workers.push_back(w);
     }
     if (!rc) {

@@ -68,6 +68,7 @@ struct Ctx {
   cudaStream_t crit = nullptr;
   cudaEvent_t ev_enter = nullptr, ev_exit = nullptr;
   cudaEvent_t ev_a = nullptr, ev_b = nullptr;
+  bool lean = false;                 // side3/side4 alias side/side2 (a batched call's worker context)
   cudaEvent_t ev_s2[6] = {};        // stage-2 bulk chains: operands prepared, A joined to B, then the
                                     // Q and Z lists of the groups using store 0 ([2], [3]) and 1 ([4], [5])
   cudaEvent_t ev[8] = {};           // stage-1 dependency events
