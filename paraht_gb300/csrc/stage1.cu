@@ -450,9 +450,9 @@ int s1_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
       cudaStreamWaitEvent(sA, evRest, 0);  // remaining-row B updates of panel k-1 done
     }
     apply_left_any(reg[0], B, ldb, P.ib(P.nblocks - 1), n - 1, GeoS1Left{P, VL[s], TL[s], 0}, P.nblocks, sA);
-    apply_left_any(reg[1], A, lda, jb0 + nb, n - 1, GeoS1Left{P, VL[s], TL[s], 1}, P.nblocks, sC);
+    apply_left_side(reg[1], A, lda, jb0 + nb, n - 1, GeoS1Left{P, VL[s], TL[s], 1}, P.nblocks, sC);
     if (!serial) cudaEventRecord(evAL, sC);
-    apply_right_any(reg[2], Q, ldq, 0, n - 1, GeoS1Q{P, VL[s], TL[s]}, P.nblocks, sC);
+    apply_right_side(reg[2], Q, ldq, 0, n - 1, GeoS1Q{P, VL[s], TL[s]}, P.nblocks, sC);
     if (timer) timer->mark(sA, 1);
     if (!serial) {
       cudaEventRecord(evLA, sA);  // B left update done: the remaining-row updates may start
@@ -508,8 +508,8 @@ int s1_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
       cudaStreamWaitEvent(sC, evPrep, 0);
     }
     apply_right_any(reg[4], A, lda, split_row, n - 1, gall, P.nblocks, sA, false);
-    apply_right_any(reg[4], A, lda, 0, split_row - 1, gall, P.nblocks, sC, false);
-    apply_right_any(reg[4], Z, ldz, 0, n - 1, gall, P.nblocks, sC, false);
+    apply_right_side(reg[4], A, lda, 0, split_row - 1, gall, P.nblocks, sC, false);
+    apply_right_side(reg[4], Z, ldz, 0, n - 1, gall, P.nblocks, sC, false);
     if (!serial) cudaEventRecord(evZ[s], sC);
   }
   if (!serial) {  // join

@@ -35,7 +35,7 @@ struct GeoS1Left {
   const double* VL;
   const double* TL;
   int onA;
-  PHT_DEV int count() const { return P.nblocks; }
+  __host__ __device__ int count() const { return P.nblocks; }
   PHT_DEV int slot_op(int s) const { return s; }
   PHT_DEV int op_slot(int o) const { return o; }
   static constexpr int kSite = 0;  // stage-1 op list (kernel statistics)
@@ -67,7 +67,7 @@ struct GeoS1Q {
   S1Panel P;
   const double* VL;
   const double* TL;
-  PHT_DEV int count() const { return P.nblocks; }
+  __host__ __device__ int count() const { return P.nblocks; }
   PHT_DEV int slot_op(int s) const { return s; }
   PHT_DEV int op_slot(int o) const { return o; }
   static constexpr int kSite = 0;  // stage-1 op list (kernel statistics)
@@ -102,7 +102,7 @@ struct GeoS1Right {
   const double* TR;
   int bl_only;  // -1: all blocks, all rows; else only block bl_only, rows [row_lo, row_hi]
   int row_lo = 0, row_hi = -1;
-  PHT_DEV int count() const { return bl_only >= 0 ? 1 : P.nblocks; }
+  __host__ __device__ int count() const { return bl_only >= 0 ? 1 : P.nblocks; }
   PHT_DEV int slot_op(int s) const { return s; }
   PHT_DEV int op_slot(int o) const { return o; }
   static constexpr int kSite = 0;  // stage-1 op list (kernel statistics)

@@ -148,12 +148,12 @@ int s2_run(Ctx& ctx, int n, double* A, int lda, double* B, int ldb, double* Q, i
       cudaStreamWaitEvent(sq, ctx.ev_a, 0);  // the chase and lookahead of this group are done
       cudaStreamWaitEvent(sz, ctx.ev_a, 0);
     }
-    apply_right_any(reg[0], B, ldb, 0, n - 1, gr, nblocks, su, false);
-    apply_left_any(reg[1], B, ldb, J, n - 1, gl, nblocks, su, false);
-    apply_right_any(reg[0], A, lda, 0, n - 1, gr, nblocks, sa, false);
-    apply_left_any(reg[1], A, lda, J, n - 1, gl, nblocks, sa, false);
-    apply_right_any(reg[2], Q, ldq, 0, n - 1, gq, nblocks, sq);
-    apply_right_any(reg[3], Z, ldz, 0, n - 1, gz, nblocks, sz);
+    apply_right_side(reg[0], B, ldb, 0, n - 1, gr, nblocks, su, false);
+    apply_left_side(reg[1], B, ldb, J, n - 1, gl, nblocks, su, false);
+    apply_right_side(reg[0], A, lda, 0, n - 1, gr, nblocks, sa, false);
+    apply_left_side(reg[1], A, lda, J, n - 1, gl, nblocks, sa, false);
+    apply_right_side(reg[2], Q, ldq, 0, n - 1, gq, nblocks, sq);
+    apply_right_side(reg[3], Z, ldz, 0, n - 1, gz, nblocks, sz);
     if (su != sa) {  // A joins B (the next lookahead's dependency); Q and Z run on
       cudaEventRecord(ctx.ev_s2[1], sa);
       cudaStreamWaitEvent(su, ctx.ev_s2[1], 0);

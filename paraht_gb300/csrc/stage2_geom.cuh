@@ -25,8 +25,8 @@ struct GeoS2 {
   // (the split-precision kernel, wy_stream.cuh).  blk = 0: the reference's op sequence with
   // the single reflectors as separate ops (FP64 kernels).
   int blk = 0;
-  PHT_DEV bool per_refl() const { return !blk && (kind == kLaRight || kind == kUpRight); }
-  PHT_DEV int count() const { return per_refl() ? nblocks * nq : nblocks; }
+  __host__ __device__ bool per_refl() const { return !blk && (kind == kLaRight || kind == kUpRight); }
+  __host__ __device__ int count() const { return per_refl() ? nblocks * nq : nblocks; }
   PHT_DEV int slot_op(int s) const { return s; }
   PHT_DEV int op_slot(int o) const { return o; }
   // Whether some row stops before the block's last reflector (the lookahead staircase): the

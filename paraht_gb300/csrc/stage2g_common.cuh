@@ -87,7 +87,7 @@ enum S2GKind {
 struct GeoS2G {
   S2GStore S;
   int n, J, r, nq, nblocks, kind;
-  PHT_DEV int count() const { return nblocks; }
+  __host__ __device__ int count() const { return nblocks; }
   PHT_DEV int slot_op(int s) const { return s; }
   PHT_DEV int op_slot(int o) const { return o; }
   static constexpr int kSite = 1;  // stage-2 op list (kernel statistics)
