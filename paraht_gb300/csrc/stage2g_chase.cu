@@ -26,7 +26,10 @@
 //     (:856-870, :942-956), one row per thread;
 //  6. the step's rotations multiplied into U(ib) and V(ib) (:970-1003) and the right ones stored
 //     as (c, s) for the staircase updates.
-// Synchronisation (progress words, ticket, bounded waits) is that of the Householder chase.
+// Within a step, warp 0 forms the rotations (2-4) and publishes each one through a flag in shared
+// memory as it is formed; the other warps apply them meanwhile (5-6), waiting (bounded) for each
+// rotation in the order the chain forms them.  Synchronisation between sweeps (progress words,
+// ticket, bounded waits) is that of the Householder chase.
 // Compiled with -Xptxas -dlcm=cg so that global loads bypass L1 and observe the other CTAs'
 // writes after the acquire.
 #include "../../include/paraht.h"
@@ -61,11 +64,28 @@ struct GSm {
   double* sv;   // r
   double* vec;  // 2 ldu: columns of the delayed left application
   int* abort_flag;
+  int* rflag;   // rflag[ig] = the step's tick once right rotation ig is in cv, sv; rflag[0]: cu, su
   int ldr;
 };
 
+// Waits until flag == tick (a value warp 0 stores after publishing the data it guards), at most
+// spin_limit polls; on timeout the chase's status word reports PARAHT_ERR_TIMEOUT and the wait
+// returns false.  Every lane of the calling warp waits for the same flag.
+static __device__ bool g_wait_flag(const int* flag, int tick, const GChaseArgs& a) {
+  long long it = 0;
+  while (*(volatile const int*)flag != tick) {
+    if (++it > a.spin_limit) {
+      atomicCAS(a.sync.status, 0, PARAHT_ERR_TIMEOUT);
+      return false;
+    }
+  }
+  __threadfence_block();
+  return true;
+}
+
+constexpr int kGFlags = 33;  // rflag entries (r <= 32, plus the left rotations')
 inline size_t g_chase_smem_bytes(int r, int nq) {
-  return sizeof(double) * ((size_t)r * (r + 1) + 4 * (size_t)r + 2 * (size_t)(r + nq));
+  return sizeof(double) * ((size_t)r * (r + 1) + 4 * (size_t)r + 2 * (size_t)(r + nq)) + sizeof(int) * kGFlags;
 }
 
 static __device__ bool g_wait(const GChaseArgs& a, int ic, int need, int* abort_flag) {
@@ -129,18 +149,24 @@ static __device__ void g_delayed_left(const S2GStore& S, int ib, int m, double* 
 // (0-based), held in registers (w[j] = column ic-1+j).
 template <int R, bool kLeft>
 static __device__ __noinline__ void g_accumulate(double* G, int ldu, int ic, int nb, const double* cs,
-                                                 const double* sns, int lane) {
+                                                 const double* sns, int lane, const int* rflag = nullptr,
+                                                 int tick = 0, const GChaseArgs* a = nullptr) {
   for (int row = lane; row < ldu; row += 32) {
     double* Gr = G + row + (size_t)(ic - 1) * ldu;
     double w[R];
 #pragma unroll
     for (int j = 0; j < R; ++j) w[j] = j < nb ? Gr[(size_t)j * ldu] : 0.0;
     double carry = w[R - 1];
+    int ready = R;  // rotations ig >= ready are known to be published
 #pragma unroll
     for (int ig = R - 1; ig >= 1; --ig) {
       if (ig > nb - 1) {
         carry = w[ig - 1];
         continue;
+      }
+      if (rflag && ig < ready) {  // the rotation chain publishes ig = nb-1 .. 1 in this order
+        g_wait_flag(rflag + ig, tick, *a);
+        ready = ig;
       }
       const double c = cs[ig], sn = sns[ig];
       const double v = w[ig - 1];
@@ -163,7 +189,9 @@ static __device__ __noinline__ void g_accumulate(double* G, int ldu, int ic, int
 // t0 + k * stride), columns p0 .. p0+nb-1 held in R registers per row.
 template <int R>
 static __device__ __noinline__ void g_rows_right(double* X, int ld, int row0, int rows, int p0, int nb, const double* cv,
-                                                 const double* sv, int t0, int stride) {
+                                                 const double* sv, int t0, int stride, const int* rflag, int tick,
+                                                 const GChaseArgs& a, int& ready) {
+  // ready: rotations ig >= ready are known to be published (ig = nb-1 .. 1 in this order)
   for (int e = t0; e < rows; e += stride) {
     double* row = X + (size_t)(row0 + e - 1) + (size_t)(p0 - 1) * ld;
     double v[R];
@@ -175,6 +203,10 @@ static __device__ __noinline__ void g_rows_right(double* X, int ld, int row0, in
       if (ig > nb - 1) {
         carry = v[ig - 1];
         continue;
+      }
+      if (ig < ready) {
+        g_wait_flag(rflag + ig, tick, a);
+        ready = ig;
       }
       const double c = cv[ig], sn = sv[ig];
       const double yv = v[ig - 1];
@@ -234,6 +266,12 @@ static __device__ void g_run_sweep(const GChaseArgs& a, int ic, GSm& s) {
       s.Bc[i * ldr + j] = B1(p0 + i, p0 + j);
     }
     __syncthreads();
+    // tick: unique per (sweep, step) within the CTA (the sequential mode runs every sweep in one CTA)
+    const int tick = (ic << 16) + ib;
+    // Warp 0 runs the step's serial part (2-4) and publishes each rotation as it forms it: the
+    // left ones after 2 (rflag[0]), right rotation ig after forming it (rflag[ig]).  Warps 1..
+    // consume them meanwhile, in the order they are formed: warp 1 multiplies the left ones into
+    // U(ib), warp 2 the right ones into V(ib), warps 3.. apply the right ones to the rows (5-6).
     if (t < 32) {
       // 2. rotations reducing the column; lane L holds element L (row p0+L)
       const double x = lane < nb ? A1(p0 + lane, cA) : 0.0;
@@ -264,6 +302,10 @@ static __device__ void g_run_sweep(const GChaseArgs& a, int ic, GSm& s) {
       }
       if (lane < nb) A1(p0 + lane, cA) = lane == 0 ? rk : 0.0;
       __syncwarp();
+      if (lane == 0) {
+        __threadfence_block();
+        *(volatile int*)&s.rflag[0] = tick;
+      }
       // 3. left rotations on the B block, one column per lane (:840-843)
       if (lane < nb) {
         double carry = s.Bc[(nb - 1) * ldr + lane];
@@ -293,39 +335,38 @@ static __device__ void g_run_sweep(const GChaseArgs& a, int ic, GSm& s) {
         if (lane == 0) {
           s.cv[ig] = c;
           s.sv[ig] = sn;
+          __threadfence_block();
+          *(volatile int*)&s.rflag[ig] = tick;
         }
         __syncwarp();
       }
-    }
-    __syncthreads();
-    for (int e = t; e < nb * nb; e += nt) {
-      const int i = e / nb, j = e % nb;
-      B1(p0 + i, p0 + j) = s.Bc[i * ldr + j];
-    }
-    // 5. right rotations on the A window and the rows above of A and B, one row per thread
-    {
-      const int nA = min(n, p0 + r + nb - 1) - p0 + 1, nAbove = p0 - istart;
-      const int total = nA + 2 * nAbove;
-      // one flat index over the three row ranges, so that every thread has a row
-      for (int e0 = 0; e0 < total; e0 += nt) {
-        const int e = e0 + t;
-        if (e < nA)
-          g_rows_right<R>(A, lda, p0 + e, 1, p0, nb, s.cv, s.sv, 0, 1);
-        else if (e < nA + nAbove)
-          g_rows_right<R>(A, lda, istart + e - nA, 1, p0, nb, s.cv, s.sv, 0, 1);
-        else if (e < total)
-          g_rows_right<R>(B, ldb, istart + e - nA - nAbove, 1, p0, nb, s.cv, s.sv, 0, 1);
+      for (int e = lane; e < nb * nb; e += 32) {
+        const int i = e / nb, j = e % nb;
+        B1(p0 + i, p0 + j) = s.Bc[i * ldr + j];
       }
-    }
-    // 6. the step's rotations into U(ib), V(ib) (:970-1003), the right ones kept as (c, s)
-    if (t < 32) {
-      g_accumulate<R, true>(S.U + S.gi(1, 1, ib), ldu, ic, nb, s.cu, s.su, lane);
     } else if (t < 64) {
-      g_accumulate<R, false>(S.V + S.gi(1, 1, ib), ldu, ic, nb, s.cv, s.sv, lane);
-    } else if (t < 64 + 32) {
-      for (int ig = t - 64 + 1; ig <= nb - 1; ig += 32) {
+      // 6. the left rotations into U(ib) (:970-984)
+      if (g_wait_flag(s.rflag, tick, a)) g_accumulate<R, true>(S.U + S.gi(1, 1, ib), ldu, ic, nb, s.cu, s.su, lane);
+    } else if (t < 96) {
+      // 6. the right rotations into V(ib) (:990-1003), then kept as (c, s) for the staircase updates
+      g_accumulate<R, false>(S.V + S.gi(1, 1, ib), ldu, ic, nb, s.cv, s.sv, lane, s.rflag, tick, &a);
+      for (int ig = lane + 1; ig <= nb - 1; ig += 32) {
         S.CV[S.ri(ic + ig - 1, ic, ib)] = s.cv[ig];
         S.SV[S.ri(ic + ig - 1, ic, ib)] = s.sv[ig];
+      }
+    } else {
+      // 5. right rotations on the A window and the rows above of A and B, one row per thread
+      const int nA = min(n, p0 + r + nb - 1) - p0 + 1, nAbove = p0 - istart;
+      const int total = nA + 2 * nAbove, nc = nt - 96;
+      int ready = R;
+      // one flat index over the three row ranges, so that every thread has a row
+      for (int e = t - 96; e < total; e += nc) {
+        if (e < nA)
+          g_rows_right<R>(A, lda, p0 + e, 1, p0, nb, s.cv, s.sv, 0, 1, s.rflag, tick, a, ready);
+        else if (e < nA + nAbove)
+          g_rows_right<R>(A, lda, istart + e - nA, 1, p0, nb, s.cv, s.sv, 0, 1, s.rflag, tick, a, ready);
+        else
+          g_rows_right<R>(B, ldb, istart + e - nA - nAbove, 1, p0, nb, s.cv, s.sv, 0, 1, s.rflag, tick, a, ready);
       }
     }
     __syncthreads();
@@ -347,8 +388,10 @@ __global__ void __launch_bounds__(kGChaseThreads, 1) k_s2g_chase(GChaseArgs a) {
   s.cv = s.su + a.r;
   s.sv = s.cv + a.r;
   s.vec = s.sv + a.r;
+  s.rflag = reinterpret_cast<int*>(s.vec + 2 * (a.r + a.nq));
   s.abort_flag = &s_abort;
   if (threadIdx.x == 0) s_abort = 0;
+  for (int i = threadIdx.x; i < kGFlags; i += blockDim.x) s.rflag[i] = 0;
   if (!a.pipelined) {
     __syncthreads();
     for (int ic = 1; ic <= a.nq; ++ic) g_run_sweep<R>(a, ic, s);
