@@ -81,7 +81,9 @@ def ht(A, B, precision="split", params=None):
     """Hessenberg-triangular form of the pencil (A, B), B upper triangular, as new arrays:
     returns (H, T, Q, Z) with H = Q^T A Z upper Hessenberg and T = Q^T B Z upper triangular.
     `precision` "split" (split-precision bulk updates) or "fp64"; `params` (r, p, nq) or None for
-    the autotuner's choice for this size (paraht_gb300.tune).  Inputs are not modified."""
+    the autotuner's choice for this size (paraht_gb300.tune), which also picks the stage-2 variant
+    (Givens rotations or small reflectors) measured faster for the precision.  Inputs are not
+    modified."""
     from . import tune
 
     if precision not in ("split", "fp64"):
@@ -101,7 +103,10 @@ def ht(A, B, precision="split", params=None):
     if n == 0:
         return H, T, Q, Z
     r, p, nq = params if params is not None else tune.pick(n, precision)
-    reduce(H, T, Q, Z, r, p, nq, PARAHT_FLAG_SPLIT if precision == "split" else 0)
+    flags = PARAHT_FLAG_SPLIT if precision == "split" else 0
+    if tune.stage2(precision, r, nq) == "givens":
+        flags |= PARAHT_FLAG_GIVENS
+    reduce(H, T, Q, Z, r, p, nq, flags)
     return H, T, Q, Z
 
 

@@ -10,13 +10,18 @@ for each mode:
   one CTA per pencil, p r <= 64), throughput in pencils/s.
 
 ``pick(n, mode)`` returns the entry of the nearest measured size (log scale); sizes outside the
-table take the nearest end.  ``python -m paraht_gb300.tune`` measures a new table:
+table take the nearest end.  ``stage2(mode, r, nq)`` names the faster stage-2 variant for a mode
+("givens", rht2ht_givens, or "householder", rht2ht_householder), from the table's measured
+comparison, where the Givens variant takes the parameters.  ``python -m paraht_gb300.tune``
+measures a new table:
 
     python -m paraht_gb300.tune --mode split --sizes 1000,2000,4000 --out paraht_gb300/tune_table.json
 
 Each candidate is timed after one untimed call of the same shape (CUDA events on the context's
 stream, inputs restored between calls outside the timed region).  The split kernel's slice count
-is fixed (8 digits of 7 bits: 36 digit products reproduce an FP64 product), so it is not tuned.
+is fixed, not tuned: 8 digits of 7 bits with the 43 digit-pair products of level t + u <= 8;
+dropping level 8 (36 products) measured a backward error of 1.5e-13 at n = 4000, above the split
+path's 1e-13 bound.
 """
 from __future__ import annotations
 
@@ -38,6 +43,11 @@ FALLBACK = {
     "batch": [[256, 16, 4, 16]],
 }
 
+# stage-2 variant per mode when the table has none: the measured comparison at n = 4000 (one
+# pencil, r=16 p=4 nq=16): split 6.67 s with Givens rotations vs 8.01 s with small reflectors;
+# FP64 9.57 s with small reflectors vs 10.78 s with Givens rotations
+STAGE2_FALLBACK = {"split": "givens", "fp64": "householder", "batch": "householder"}
+
 CANDIDATES = {
     "split": [(16, 4, 16), (16, 3, 16), (16, 5, 16), (16, 4, 8), (32, 2, 16), (8, 4, 8)],
     "fp64": [(16, 4, 16), (16, 3, 16), (16, 5, 16), (16, 4, 8), (32, 2, 16), (32, 4, 16)],
@@ -52,6 +62,27 @@ def load_table(path: str = TABLE_PATH) -> dict:
         return {m: t.get(m, FALLBACK[m]) or FALLBACK[m] for m in FALLBACK}
     except (OSError, ValueError):
         return dict(FALLBACK)
+
+
+def stage2(mode: str = "split", r: int = 16, nq: int = 16, table: dict | None = None) -> str:
+    """The faster stage-2 variant for `mode`: "givens" or "householder".  The Givens variant needs
+    r <= 32 and r + nq <= 64 (split-precision dense ops up to 48 wide), and the persistent batched
+    kernel chases with reflectors only."""
+    if mode not in FALLBACK:
+        raise ValueError(f"unknown mode {mode!r}")
+    t = table if table is not None else _raw_table()
+    choice = (t.get("stage2") or {}).get(mode, STAGE2_FALLBACK[mode])
+    if choice == "givens" and (mode == "batch" or r > 32 or r + nq > 64):
+        return "householder"
+    return choice
+
+
+def _raw_table(path: str = TABLE_PATH) -> dict:
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
 
 
 def pick(n: int, mode: str = "split", table: dict | None = None):

@@ -27,3 +27,15 @@ def test_missing_table_falls_back(tmp_path):
     assert set(t) == {"split", "fp64", "batch"}
     r, p, nq = tune.pick(16000, "split", t)
     assert 1 <= nq <= r and p >= 2
+
+
+def test_stage2_variant_per_mode(tmp_path):
+    table = {"split": [[1000, 16, 4, 16]], "fp64": [[1000, 32, 4, 16]], "batch": [[256, 16, 4, 16]],
+             "stage2": {"split": "givens", "fp64": "householder"}}
+    assert tune.stage2("split", 16, 16, table) == "givens"
+    assert tune.stage2("fp64", 32, 16, table) == "householder"
+    assert tune.stage2("batch", 16, 16, table) == "householder"  # the persistent kernel chases with reflectors
+    assert tune.stage2("split", 48, 8, table) == "householder"   # the Givens variant needs r <= 32
+    assert tune.stage2("split", 32, 40, table) == "householder"  # ... and r + nq <= 64
+    assert tune.stage2("split", 16, 16, {}) == "givens"          # no table entry: the measured default
+    assert tune.stage2("split", 16, 16) in ("givens", "householder")  # the shipped table
