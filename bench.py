@@ -23,7 +23,8 @@ and the CPU baselines.  ``steps`` is the number of split reductions actually tim
   variant (small reflectors), its backward errors, and ``split_vs_fp64`` = fp64 seconds / split
   seconds.  The split path runs its faster stage-2 variant, Givens rotations (--stage2).
 * ``check``: backward errors ||Q^T A0 Z - H||/||A0||, ||Q^T B0 Z - T||/||B0|| and orthogonality
-  ||Q^T Q - I||_F, ||Z^T Z - I||_F of the last split step (FP64 GEMMs on the device).
+  ||Q^T Q - I||_F, ||Z^T Z - I||_F of the last split step (FP64 GEMMs on the device); ``eig``: the
+  generalized eigenvalues of a seeded n=600 pencil against those of its (H, T) from each arm.
 * ``e2e``: one split reduction through the public host entry point paraht_reduce_host with
   pinned host buffers, host<->device copies inside the timed region.
 * ``roofline``: the dominant kernel (the split-precision op-list kernel of stage 2), every launch
@@ -526,6 +527,51 @@ def device_check(torch, work, dev0):
     return out
 
 
+def eig_mismatch(l1, l2) -> float:
+    """Largest distance from an eigenvalue of l1 to its greedy nearest match in l2 (each used
+    once), relative to max(1, |lambda|); infinite eigenvalues must match infinite ones."""
+    a = np.asarray(l1, dtype=complex)
+    b = np.asarray(l2, dtype=complex)
+    if a.shape != b.shape:
+        return float("inf")
+    free = np.ones(b.shape[0], dtype=bool)
+    worst = 0.0
+    for lam in a:
+        if not np.isfinite(lam):
+            idx = np.flatnonzero(free & ~np.isfinite(b))
+            if idx.size == 0:
+                return float("inf")
+            free[idx[0]] = False
+            continue
+        d = np.where(free & np.isfinite(b), np.abs(b - lam), np.inf)
+        i = int(np.argmin(d))
+        if not np.isfinite(d[i]):
+            return float("inf")
+        free[i] = False
+        worst = max(worst, float(d[i]) / max(1.0, abs(lam)))
+    return worst
+
+
+def eig_check(ctx, arms, n_e: int = 600, seed: int = 7) -> dict:
+    """Generalized eigenvalues of a seeded n_e pencil (LAPACK DGGEV through scipy) against those of
+    its Hessenberg-triangular forms from each arm, reduced through the host entry point:
+    arms = [(name, (r, p, nq), flags)].  The largest relative distance per arm."""
+    import scipy.linalg as sla
+
+    from paraht_gb300.generate import identity, pencil
+
+    A0, B0 = pencil(n_e, "std", seed=seed)
+    ref = sla.eigvals(A0, B0)
+    out = {"n": n_e, "method": "scipy.linalg.eigvals (LAPACK DGGEV) of (A0, B0) vs of (H, T), greedy matching, "
+                               "relative to max(1, |lambda|)"}
+    for name, (r, p, nq), fl in arms:
+        H, T = np.asfortranarray(A0.copy()), np.asfortranarray(B0.copy())
+        Q, Z = identity(n_e), identity(n_e)
+        ctx.reduce_host(H, T, Q, Z, r, p, nq, fl)
+        out[name] = float(eig_mismatch(ref, sla.eigvals(H, T)))
+    return out
+
+
 def run_pencil(args, rank: int, world: int, local: int):
     import torch
 
@@ -685,6 +731,14 @@ def run_pencil(args, rank: int, world: int, local: int):
         check = device_check(torch, work, dev0)
         check["bound_split"] = 1e-13
         check["bound_10n_eps"] = 10 * n * EPS
+        if rank == 0 and not stage2_only:  # eigenvalues of a small pencil through both arms (a few seconds)
+            arms = [(args.precision, (r, p, nq), flags & ~ph.PARAHT_FLAG_KERNEL_TIMES)]
+            if do_fp64:
+                arms.append(("fp64", (fr, fp, fnq), fvariant))
+            try:
+                check["eig"] = eig_check(ctx, arms)
+            except Exception as exc:  # the line keeps its timing even if this check cannot run
+                check["eig"] = {"error": f"{type(exc).__name__}: {exc}"[:200]}
 
     # end to end through the host entry point, copies inside the timed region
     hbuf = [torch.empty((n, n), dtype=torch.float64).pin_memory() for _ in range(4)] if args.e2e_steps > 0 else []

@@ -5,6 +5,8 @@ import os
 import subprocess
 import sys
 
+import pytest
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
@@ -51,3 +53,16 @@ def test_budget_plan():
     assert not bench.budget_plan(1500.0, 10.0, 1.0, 20, 20, 0.0)  # all requested steps done
     args = bench.parse(["--steps", "20", "--warmup", "5"])
     assert args.budget_s + 0 <= 1700 and args.n == 16000 and args.fp64_params == "32,4,16"
+
+
+def test_eig_mismatch_greedy_matching():
+    import numpy as np
+
+    sys.path.insert(0, ROOT)
+    import bench
+
+    assert bench.eig_mismatch([1.0, 2.0, np.inf], [2.0, np.inf, 1.0]) == 0.0
+    assert abs(bench.eig_mismatch([1.0, 200.0], [1.0, 202.0]) - 0.01) < 1e-15  # relative to |lambda|
+    assert bench.eig_mismatch([0.5], [0.6]) == pytest.approx(0.1)           # absolute below |lambda| = 1
+    assert bench.eig_mismatch([1.0, np.inf], [1.0, 2.0]) == float("inf")    # an infinite one unmatched
+    assert bench.eig_mismatch([1.0], [1.0, 2.0]) == float("inf")
