@@ -67,6 +67,27 @@ def test_null_pointer_and_stage_entry_errors():
     assert L.paraht_reduce(*([0] + args[1:])) == 0  # n = 0: quick return
 
 
+def test_givens_entry_rejects_before_the_gpu():
+    L = _lib.lib()
+    A, args = _args()
+    # rht2ht_givens: (n, A, lda, B, ldb, Q, ldq, Z, ldz, r, nq)
+    assert L.paraht_rht2ht_givens(*(args[:9] + [4, 9])) == -11  # nq > r, outside the reference's valid domain
+    assert L.paraht_rht2ht_givens(*(args[:9] + [40, 8])) == -1005  # r > 32: PARAHT_ERR_NOT_SUPPORTED
+    assert L.paraht_rht2ht_givens(*([0] + args[1:9] + [4, 4])) == 0  # n = 0: quick return
+
+
+def test_batch_plan_entry_points_reject_bad_handles():
+    L = _lib.lib()
+    assert L.paraht_batch_plan_create(None, 0, None, None, None, None, None, None, None, None, None, None, None,
+                                      None, 0, None) == -16  # no place for the plan handle
+    plan = C.c_void_p()
+    assert L.paraht_batch_plan_create(None, 0, None, None, None, None, None, None, None, None, None, None, None,
+                                      None, 0, C.byref(plan)) == -1007  # no context
+    assert plan.value is None
+    assert L.paraht_batch_plan_launch(None, None) == -1007
+    assert L.paraht_batch_plan_destroy(None) == -1007
+
+
 def test_context_entry_points_reject_bad_context():
     L = _lib.lib()
     A, args = _args()

@@ -117,3 +117,18 @@ def test_oracle_givens_stage2(oracle, n, r, p, nq):
     oracle.rht2ht_householder(Ah, Bh, Qh, Zh, r, nq)
     assert abs_rel_max_diff(np.triu(Ag, -1), np.triu(Ah, -1)) < 1e-10
     assert abs_rel_max_diff(np.triu(Bg), np.triu(Bh)) < 1e-10
+
+
+@pytest.mark.parametrize("r", [4, 8, 16])
+@pytest.mark.parametrize("n", [97, 160, 203, 240])
+def test_oracle_givens_domain_nq_r_plus_1(oracle, n, r):
+    """The Givens stage 2 is exact up to nq = r + 1, the edge of the domain the library accepts
+    for both stage-2 variants (nq <= r; the reference's own index bookkeeping goes wrong for some n
+    once nq exceeds r + 1 by more)."""
+    nq = r + 1
+    A0, B0 = make(n)
+    S1 = oracle_reduce(oracle, A0, B0, r, 4, r, stage=1)
+    A, B, Q, Z = copies(*S1)
+    oracle.rht2ht_givens(A, B, Q, Z, r, nq)
+    tol = 10 * n * EPS
+    assert bwd(Q, A0, Z, A) <= tol and bwd(Q, B0, Z, B) <= tol
