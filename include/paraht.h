@@ -207,6 +207,27 @@ int paraht_gghd3_d(paraht_ctx ctx, char compq, char compz, int n, int ilo, int i
 int paraht_gghd3(char compq, char compz, int n, int ilo, int ihi, double* A, int lda, double* B, int ldb, double* Q,
                  int ldq, double* Z, int ldz, int r, int p, int nq, int flags);
 
+/* ---- generalized eigenvalues of Hessenberg-triangular pencils: the QZ iteration that consumes
+ * the reduced pencil (LAPACK DHGEQZ with JOB='E', COMPQ=COMPZ='N'; no counterpart in the
+ * reference, whose driver stops at the reduced pencil, src/profilereduction.f90:156).
+ * For i < count: H[i] (n[i] x n[i], leading dimension ldh[i]) upper Hessenberg and T[i] (ldt[i])
+ * upper triangular, read only (entries below the structure are ignored).  Eigenvalue j of pencil
+ * i is (alphar[i][j] + i alphai[i][j]) / beta[i][j] with beta >= 0, in the order of the Schur
+ * form's diagonal.  Complex single-shift QZ (Moler-Stewart, Wilkinson shifts), one warp per
+ * pencil: the eigenvalues of a real pencil come out with rounding-level imaginary parts where
+ * DHGEQZ returns exact zeros and exact conjugate pairs.  info[i] (host array): 0; 1 when a
+ * diagonal entry of T is at most eps ||T||_F (an infinite or nearly infinite eigenvalue: not
+ * supported, that pencil's outputs are not written); 2 when 30 n[i] sweeps did not converge.
+ * _d: host arrays of device pointers, run on the context's stream and synchronised; the plain
+ * form takes host arrays on this thread's default context.  Status: 0; -2 count < 0, -3 an
+ * n < 0 (or null n), -4 .. -10 a null pointer among H, ldh, T, ldt, alphar, alphai, beta (ldh,
+ * ldt: or below max(1, n)), -11 null info; else a PARAHT_ERR_ code (both forms). ---- */
+int paraht_hgeqz_eigs_d(paraht_ctx ctx, int count, const int* n, const double* const* H, const int* ldh,
+                        const double* const* T, const int* ldt, double* const* alphar, double* const* alphai,
+                        double* const* beta, int* info);
+int paraht_hgeqz_eigs(int count, const int* n, const double* const* H, const int* ldh, const double* const* T,
+                      const int* ldt, double* const* alphar, double* const* alphai, double* const* beta, int* info);
+
 /* ---- failure-path self-test (no counterpart in the reference) ----
  * Runs the pipelined chase's bounded device-side wait on a progress word that nothing sets, with
  * a limit of spin_limit polls (1 .. 2^20, about 1 us each).  Returns the status the kernel

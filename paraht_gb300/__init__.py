@@ -29,7 +29,8 @@ from ._lib import (PARAHT_BATCH_MAX_N, PARAHT_FLAG_BATCH_LOOP, PARAHT_FLAG_CHECK
                    PARAHT_FLAG_TIME_CHAIN, PARAHT_FLAG_TIME_COMPONENTS, ParahtError, check, lib)
 
 __all__ = [
-    "ab2rht_simple", "rht2ht_householder", "rht2ht_givens", "reduce", "ht", "gghd3", "Context", "BatchPlan",
+    "ab2rht_simple", "rht2ht_householder", "rht2ht_givens", "reduce", "ht", "gghd3", "hgeqz_eigs", "Context",
+    "BatchPlan",
     "ParahtError",
     "PARAHT_FLAG_TIME_COMPONENTS", "PARAHT_FLAG_CHECK_FINITE", "PARAHT_FLAG_SPLIT", "PARAHT_FLAG_NO_ZERO_FILL",
     "PARAHT_FLAG_SEQUENTIAL", "PARAHT_FLAG_KERNEL_TIMES", "PARAHT_FLAG_BATCH_LOOP", "PARAHT_FLAG_GIVENS",
@@ -121,6 +122,34 @@ def gghd3(compq, compz, ilo, ihi, A, B, Q, Z, r=16, p=4, nq=16, flags=0):
           "gghd3")
 
 
+def hgeqz_eigs(H, T):
+    """Generalized eigenvalues of Hessenberg-triangular pencils by the QZ iteration on the GPU
+    (LAPACK DHGEQZ with JOB='E'; paraht_hgeqz_eigs), the step after the reduction.  H, T: one
+    pair of float64 arrays (H upper Hessenberg, T upper triangular; entries below ignored) or two
+    lists of them, reduced together.  Returns (alpha, beta, info) for one pair, else a list of
+    them: alpha complex, beta real >= 0, eigenvalue alpha / beta; info 1 (T has a negligible
+    diagonal entry: infinite eigenvalues are not supported) or 2 (no convergence) leave alpha and
+    beta None."""
+    single = not isinstance(H, (list, tuple))
+    Hs = [np.asfortranarray(h, dtype=np.float64) for h in ([H] if single else H)]
+    Ts = [np.asfortranarray(t, dtype=np.float64) for t in ([T] if single else T)]
+    if len(Hs) != len(Ts) or any(h.ndim != 2 or h.shape[0] != h.shape[1] or h.shape != t.shape
+                                 for h, t in zip(Hs, Ts)):
+        raise ValueError("H and T must be square arrays of equal shapes")
+    cnt = len(Hs)
+    ns = [h.shape[0] for h in Hs]
+    ar, ai, be = ([np.zeros(n) for n in ns] for _ in range(3))
+    info = (C.c_int * cnt)()
+    IA, PA = C.c_int * cnt, C.c_void_p * cnt
+    lds = IA(*[max(1, n) for n in ns])
+    check(lib().paraht_hgeqz_eigs(cnt, IA(*ns), PA(*[h.ctypes.data for h in Hs]), lds,
+                                  PA(*[t.ctypes.data for t in Ts]), lds, PA(*[a.ctypes.data for a in ar]),
+                                  PA(*[a.ctypes.data for a in ai]), PA(*[b.ctypes.data for b in be]), info),
+          "hgeqz_eigs")
+    out = [(ar[i] + 1j * ai[i], be[i], 0) if info[i] == 0 else (None, None, int(info[i])) for i in range(cnt)]
+    return out[0] if single else out
+
+
 class Context:
     """A libparaht context: one CUDA device, one stream, reusable workspace."""
 
@@ -193,6 +222,16 @@ class Context:
         """A BatchPlan: the persistent batched launch for these pencils captured as a CUDA graph
         (paraht_batch_plan_create); replay it with .launch(stream)."""
         return BatchPlan(self, ns, As, ldas, Bs, ldbs, Qs, ldqs, Zs, ldzs, rs, ps, nqs, flags)
+
+    def hgeqz_eigs_d(self, ns, Hs, ldhs, Ts, ldts, alphars, alphais, betas):
+        """QZ eigenvalues of Hessenberg-triangular pencils in device memory (paraht_hgeqz_eigs_d);
+        returns the per-pencil info list (0, 1 unsupported, 2 no convergence)."""
+        cnt = len(ns)
+        IA, PA = C.c_int * cnt, C.c_void_p * cnt
+        info = IA()
+        check(lib().paraht_hgeqz_eigs_d(self._h, cnt, IA(*ns), PA(*Hs), IA(*ldhs), PA(*Ts), IA(*ldts), PA(*alphars),
+                                        PA(*alphais), PA(*betas), info), "hgeqz_eigs_d")
+        return [int(v) for v in info]
 
     def selftest_wait_timeout(self, spin_limit: int = 1000) -> int:
         """Runs the chase's bounded wait on a flag nothing sets; returns the reported status

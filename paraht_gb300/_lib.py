@@ -62,6 +62,10 @@ SIGNATURES = {
     "paraht_batch_plan_destroy": [C.c_void_p],
     "paraht_gghd3": [C.c_char, C.c_char, _i, _i, _i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i, _i, _i],
     "paraht_gghd3_d": [C.c_void_p, C.c_char, C.c_char, _i, _i, _i, _d, _i, _d, _i, _d, _i, _d, _i, _i, _i, _i, _i],
+    "paraht_hgeqz_eigs_d": [C.c_void_p, _i, C.POINTER(_i), C.POINTER(_d), C.POINTER(_i), C.POINTER(_d),
+                            C.POINTER(_i), C.POINTER(_d), C.POINTER(_d), C.POINTER(_d), C.POINTER(_i)],
+    "paraht_hgeqz_eigs": [_i, C.POINTER(_i), C.POINTER(_d), C.POINTER(_i), C.POINTER(_d), C.POINTER(_i),
+                          C.POINTER(_d), C.POINTER(_d), C.POINTER(_d), C.POINTER(_i)],
     "paraht_selftest_wait_timeout": [C.c_void_p, C.c_longlong],
     "paraht_selftest_reflector": [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p],
     "paraht_strerror": [_i],

@@ -11,11 +11,13 @@
 #include <mutex>
 #include <new>
 #include <thread>
+#include <vector>
 
 #include "launch_count.h"
 #include "paraht_impl.h"
 #include "paraht_internal.cuh"
 #include "s2_common.cuh"
+#include "qz.cuh"
 #include "split_apply.cuh"
 
 namespace pht {
@@ -966,6 +968,121 @@ extern "C" int paraht_selftest_reflector(paraht_ctx c, int count, const double* 
   pht::launch_reflector_selftest(x.stream, count, alpha, xnorm2, out);
   const int rc = finish(x);
   cudaSetDevice(prev);
+  return rc;
+}
+
+// ---- generalized eigenvalues of Hessenberg-triangular pencils (QZ) ----
+static int hgeqz_check(int count, const int* n, const double* const* H, const int* ldh, const double* const* T,
+                       const int* ldt, double* const* alphar, double* const* alphai, double* const* beta,
+                       const int* info) {
+  if (count < 0) return -2;
+  if (count == 0) return 0;
+  if (!n) return -3;
+  if (!H) return -4;
+  if (!ldh) return -5;
+  if (!T) return -6;
+  if (!ldt) return -7;
+  if (!alphar) return -8;
+  if (!alphai) return -9;
+  if (!beta) return -10;
+  if (!info) return -11;
+  for (int i = 0; i < count; ++i) {
+    if (n[i] < 0) return -3;
+    const int ldmin = std::max(1, n[i]);
+    if (n[i] > 0 && !H[i]) return -4;
+    if (ldh[i] < ldmin) return -5;
+    if (n[i] > 0 && !T[i]) return -6;
+    if (ldt[i] < ldmin) return -7;
+    if (n[i] > 0 && !alphar[i]) return -8;
+    if (n[i] > 0 && !alphai[i]) return -9;
+    if (n[i] > 0 && !beta[i]) return -10;
+  }
+  return 0;
+}
+
+extern "C" int paraht_hgeqz_eigs_d(paraht_ctx c, int count, const int* n, const double* const* H, const int* ldh,
+                                   const double* const* T, const int* ldt, double* const* alphar,
+                                   double* const* alphai, double* const* beta, int* info) {
+  if (!ctx_ok(c)) return PARAHT_ERR_BAD_CTX;
+  if (const int bad = hgeqz_check(count, n, H, ldh, T, ldt, alphar, alphai, beta, info)) return bad;
+  if (count == 0) return 0;
+  std::vector<pht::QzPencil> tab((size_t)count);
+  long long work = 0;
+  for (int i = 0; i < count; ++i) {
+    tab[i] = pht::QzPencil{H[i], T[i], alphar[i], alphai[i], beta[i], work, n[i], ldh[i], ldt[i], 0};
+    work += pht::qz_work_elems(n[i]);
+  }
+  auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t tab_b = up(sizeof(pht::QzPencil) * (size_t)count), info_b = up(sizeof(int) * (size_t)count);
+  const size_t bytes = tab_b + info_b + (size_t)work * sizeof(pht::QzC);
+  Ctx& x = c->c;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(x.device);
+  char* buf = nullptr;
+  if (cudaMalloc(&buf, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    cudaSetDevice(prev);
+    return PARAHT_ERR_ALLOC;
+  }
+  auto* dtab = reinterpret_cast<pht::QzPencil*>(buf);
+  auto* dinfo = reinterpret_cast<int*>(buf + tab_b);
+  auto* dwork = reinterpret_cast<pht::QzC*>(buf + tab_b + info_b);
+  cudaMemcpyAsync(dtab, tab.data(), sizeof(pht::QzPencil) * (size_t)count, cudaMemcpyHostToDevice, x.stream);
+  pht::launch_qz_eigs(x.stream, dtab, count, dwork, dinfo);
+  cudaMemcpyAsync(info, dinfo, sizeof(int) * (size_t)count, cudaMemcpyDeviceToHost, x.stream);
+  const int rc = finish(x);
+  cudaFree(buf);
+  cudaSetDevice(prev);
+  return rc;
+}
+
+extern "C" int paraht_hgeqz_eigs(int count, const int* n, const double* const* H, const int* ldh,
+                                 const double* const* T, const int* ldt, double* const* alphar, double* const* alphai,
+                                 double* const* beta, int* info) {
+  if (const int bad = hgeqz_check(count, n, H, ldh, T, ldt, alphar, alphai, beta, info)) return bad;
+  if (count == 0) return 0;
+  paraht_ctx c;
+  int rc = default_ctx(&c);
+  if (rc) return rc;
+  // device copies: per pencil H, T (n x n, leading dimension n) and the three output vectors
+  std::vector<long long> off((size_t)count + 1, 0);
+  for (int i = 0; i < count; ++i) off[i + 1] = off[i] + 2ll * n[i] * n[i] + 3ll * n[i];
+  double* d = nullptr;
+  if (cudaMalloc(&d, sizeof(double) * (size_t)std::max(1ll, off[count])) != cudaSuccess) {
+    cudaGetLastError();
+    return PARAHT_ERR_ALLOC;
+  }
+  std::vector<const double*> dH(count), dT(count);
+  std::vector<double*> dar(count), dai(count), dbe(count);
+  std::vector<int> ld(count);
+  for (int i = 0; i < count && !rc; ++i) {
+    const size_t m = (size_t)n[i];
+    double* p = d + off[i];
+    dH[i] = p;
+    dT[i] = p + m * m;
+    dar[i] = p + 2 * m * m;
+    dai[i] = dar[i] + m;
+    dbe[i] = dai[i] + m;
+    ld[i] = std::max(1, n[i]);
+    if (m && (cudaMemcpy2D(p, m * sizeof(double), H[i], (size_t)ldh[i] * sizeof(double), m * sizeof(double), m,
+                           cudaMemcpyHostToDevice) != cudaSuccess ||
+              cudaMemcpy2D(p + m * m, m * sizeof(double), T[i], (size_t)ldt[i] * sizeof(double), m * sizeof(double),
+                           m, cudaMemcpyHostToDevice) != cudaSuccess))
+      rc = PARAHT_ERR_CUDA;
+  }
+  if (!rc) rc = paraht_hgeqz_eigs_d(c, count, n, dH.data(), ld.data(), dT.data(), ld.data(), dar.data(), dai.data(),
+                                    dbe.data(), info);
+  for (int i = 0; i < count && !rc; ++i) {
+    const size_t b = sizeof(double) * (size_t)n[i];
+    if (n[i] && info[i] == 0 &&
+        (cudaMemcpy(alphar[i], dar[i], b, cudaMemcpyDeviceToHost) != cudaSuccess ||
+         cudaMemcpy(alphai[i], dai[i], b, cudaMemcpyDeviceToHost) != cudaSuccess ||
+         cudaMemcpy(beta[i], dbe[i], b, cudaMemcpyDeviceToHost) != cudaSuccess))
+      rc = PARAHT_ERR_CUDA;
+  }
+  if (rc == PARAHT_ERR_CUDA) cudaGetLastError();
+  cudaFree(d);
   return rc;
 }
 
