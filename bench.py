@@ -90,9 +90,10 @@ def parse(argv=None):
     ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("paraht", "reference"), default="paraht")
-    ap.add_argument("--workload", choices=("pencil", "batch4096", "batch256"), default="pencil",
+    ap.add_argument("--workload", choices=("pencil", "batch4096", "batch256", "qz1216"), default="pencil",
                     help="pencil: one n x n pencil (the headline); batch4096: 4096 FP64 pencils, n ~ U{32..512}; "
-                         "batch256: 256 pencils, n log-uniform in [256, 4096], 30%% graded, split precision")
+                         "batch256: 256 pencils, n log-uniform in [256, 4096], 30%% graded, split precision; "
+                         "qz1216: QZ eigenvalues of 1216 Hessenberg-triangular pencils, n ~ U{32..256}")
     ap.add_argument("--loop-sample", type=int, default=0,
                     help="pencils of the looped baseline (batch workloads; 0: the workload's default)")
     ap.add_argument("--n", type=int, default=16000)
@@ -902,11 +903,147 @@ def run_pencil(args, rank: int, world: int, local: int):
     return 0
 
 
+def qz_pencil(n: int, seed: int):
+    """A random Hessenberg-triangular pencil: H with N(0,1) entries on and above the subdiagonal,
+    T upper triangular N(0,1) with diagonal entries of modulus 1 + |N(0,1)|."""
+    rng = np.random.default_rng(seed)
+    H = np.triu(rng.standard_normal((n, n)), -1)
+    T = np.triu(rng.standard_normal((n, n)))
+    T[np.diag_indices(n)] = np.sign(T.diagonal() + 0.5) * (1.0 + np.abs(rng.standard_normal(n)))
+    return np.asfortranarray(H), np.asfortranarray(T)
+
+
+def run_qz(args, rank: int, world: int, local: int):
+    """--workload qz1216: generalized eigenvalues of 1216 Hessenberg-triangular pencils (152 SMs x 8,
+    n ~ U{32..256}) in one paraht_hgeqz_eigs_d call, the QZ step after the reduction; LAPACK DHGEQZ
+    (the oracle's, one thread) on a sample of the same pencils is the CPU baseline."""
+    from paraht_gb300.generate import batch_sizes
+
+    count, lo, hi = 1216, 32, 256
+    sizes = batch_sizes(count, lo, hi, "uniform", seed=replica_seed(4242, rank))
+    n3 = statistics.mean(float(n) ** 3 for n in sizes)
+    metric = "QZ eigenvalues: pencils/s, 1216 Hessenberg-triangular pencils n~U{32..256}"
+    workload = (f"{count} random Hessenberg-triangular pencils, n ~U{{{lo}..{hi}}} (seeded), eigenvalues only, "
+                "one paraht_hgeqz_eigs_d call (complex single-shift QZ, a warp per pencil below n=128, a 2-warp CTA from there)")
+
+    def cpu_rate(nsample):
+        from oracle import oracle as O
+
+        O.set_blas_threads(1)
+        per, mism = [], []
+        for i in range(nsample):
+            H, T = qz_pencil(sizes[i], 9000 + i)
+            t0 = time.perf_counter()
+            ar, ai, be, info = O.dhgeqz_eigs(H, T)
+            per.append((time.perf_counter() - t0) / float(sizes[i]) ** 3)
+        v = 1.0 / (statistics.mean(per) * n3)
+        return v, {"value": v, "unit": "pencils/s", "cores": 1, "kind": "port",
+                   "sample": f"LAPACK DHGEQZ (eigenvalues only) on the first {nsample} pencils, one thread, time "
+                             f"per pencil scaled by the batch's mean n^3"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        vs = [cpu_rate(64) for _ in range(max(1, args.steps))]
+        v = statistics.mean(x[0] for x in vs)
+        print(json.dumps({
+            "metric": metric, "value": v, "unit": "pencils/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * count / v, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": workload}, "cpu_baseline": {**vs[-1][1], "value": v},
+            "e2e": {"value": v, "unit": "pencils/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}), flush=True)
+        return 0
+
+    import torch
+
+    import paraht_gb300 as ph
+
+    torch.cuda.set_device(local)
+    dist_on = world > 1
+    if dist_on:
+        import torch.distributed as td
+
+        td.init_process_group("nccl", device_id=torch.device("cuda", local))
+    host = [qz_pencil(n, 9000 + i) for i, n in enumerate(sizes)]
+    dH = [torch.from_numpy(np.ascontiguousarray(h.T)).cuda() for h, _ in host]
+    dT = [torch.from_numpy(np.ascontiguousarray(t.T)).cuda() for _, t in host]
+    out = [torch.zeros(3, n, dtype=torch.float64, device="cuda") for n in sizes]
+    ctx = ph.Context(local)
+    ptrs = ([x.data_ptr() for x in dH], [x.data_ptr() for x in dT], [o[0].data_ptr() for o in out],
+            [o[1].data_ptr() for o in out], [o[2].data_ptr() for o in out])
+
+    def call():
+        return ctx.hgeqz_eigs_d(sizes, ptrs[0], sizes, ptrs[1], sizes, ptrs[2], ptrs[3], ptrs[4])
+
+    def barrier():
+        if dist_on:
+            import torch.distributed as td
+
+            td.barrier()
+
+    for _ in range(args.warmup):
+        call()
+    ts, launches, infos = [], 0, []
+    sampler = ClockSampler(local)
+    with sampler:
+        for _ in range(args.steps):
+            barrier()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            infos = call()  # synchronous: returns after the kernel and the status copy
+            ts.append(time.perf_counter() - t0)
+            launches += ctx.launch_count()
+            barrier()
+    t_step = job_time(statistics.mean(ts), "cuda")
+    value = world * count / t_step
+    # end to end through the host entry: pencils from host memory, eigenvalues back
+    t0 = time.perf_counter()
+    res = ph.hgeqz_eigs([h for h, _ in host], [t for _, t in host])
+    e2e_v = world * count / (time.perf_counter() - t0)
+    h2d = sum(2 * 8 * n * n for n in sizes)
+    d2h = sum(3 * 8 * n for n in sizes)
+    check = None
+    cpu = None
+    if rank == 0:
+        from oracle import oracle as O
+
+        worst = 0.0
+        for i in range(32):
+            ar, ai, be, _ = O.dhgeqz_eigs(*host[i])
+            a, b, _ = res[i]
+            worst = max(worst, eig_mismatch(a / b, (ar + 1j * ai) / be))
+        check = {"pencils": 32, "eig_mismatch_vs_dhgeqz": worst, "info_nonzero": sum(1 for v in infos if v)}
+        if not args.no_cpu_baseline:
+            cpu = cpu_rate(64)[1]
+        print(json.dumps({
+            "metric": metric, "value": value, "unit": "pencils/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": {"workload": workload, "pencils": count, "n_lo": lo, "n_hi": hi,
+                       "l2": "working set about 1 GB of complex copies, above L2"},
+            "e2e": {"value": e2e_v, "unit": "pencils/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "roofline": {"bound": "fp64", "achieved": None, "peak": None, "unit": None, "frac": None,
+                         "traffic": None, "kernel": "k_qz_eigs: a warp or a 2-warp CTA per pencil; complex rotations "
+                                                      "bound by the FP64 issue rate (one warp instruction per "
+                                                      "scheduler every ~64 cycles); flops not counted"},
+            "check": check, "cpu_baseline": cpu, "clocks": sampler.summary(),
+        }), flush=True)
+    if dist_on:
+        import torch.distributed as td
+
+        td.destroy_process_group()
+    ctx.close()
+    return 0
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.workload == "qz1216":
+        return run_qz(args, rank, world, local)
     if args.workload != "pencil":
         return run_batch(args, rank, world, local)
     if args.impl == "reference":

@@ -1012,9 +1012,26 @@ extern "C" int paraht_hgeqz_eigs_d(paraht_ctx c, int count, const int* n, const 
     tab[i] = pht::QzPencil{H[i], T[i], alphar[i], alphai[i], beta[i], work, n[i], ldh[i], ldt[i], 0};
     work += pht::qz_work_elems(n[i]);
   }
+  // CTAs: the largest pencils first, each n >= kQzWholeMin on a CTA of its own, the rest one per
+  // warp in decreasing size
+  std::vector<int> order((size_t)count);
+  for (int i = 0; i < count; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return n[a] > n[b]; });
+  std::vector<pht::QzBlock> blocks;
+  for (size_t k = 0; k < order.size();) {
+    pht::QzBlock b{{-1, -1, -1, -1}, 0};
+    if (n[order[k]] >= pht::kQzWholeMin) {
+      b.pencil[0] = order[k++];
+      b.whole = 1;
+    } else {
+      for (int w = 0; w < pht::kQzThreads / 32 && k < order.size(); ++w) b.pencil[w] = order[k++];
+    }
+    blocks.push_back(b);
+  }
   auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
   const size_t tab_b = up(sizeof(pht::QzPencil) * (size_t)count), info_b = up(sizeof(int) * (size_t)count);
-  const size_t bytes = tab_b + info_b + (size_t)work * sizeof(pht::QzC);
+  const size_t blk_b = up(sizeof(pht::QzBlock) * blocks.size());
+  const size_t bytes = tab_b + info_b + blk_b + (size_t)work * sizeof(pht::QzC);
   Ctx& x = c->c;
   int prev = 0;
   cudaGetDevice(&prev);
@@ -1027,9 +1044,13 @@ extern "C" int paraht_hgeqz_eigs_d(paraht_ctx c, int count, const int* n, const 
   }
   auto* dtab = reinterpret_cast<pht::QzPencil*>(buf);
   auto* dinfo = reinterpret_cast<int*>(buf + tab_b);
-  auto* dwork = reinterpret_cast<pht::QzC*>(buf + tab_b + info_b);
+  auto* dblk = reinterpret_cast<pht::QzBlock*>(buf + tab_b + info_b);
+  auto* dwork = reinterpret_cast<pht::QzC*>(buf + tab_b + info_b + blk_b);
   cudaMemcpyAsync(dtab, tab.data(), sizeof(pht::QzPencil) * (size_t)count, cudaMemcpyHostToDevice, x.stream);
-  pht::launch_qz_eigs(x.stream, dtab, count, dwork, dinfo);
+  cudaMemcpyAsync(dblk, blocks.data(), sizeof(pht::QzBlock) * blocks.size(), cudaMemcpyHostToDevice, x.stream);
+  const long long l0 = pht::tl_launches;
+  pht::launch_qz_eigs(x.stream, dtab, dblk, (int)blocks.size(), dwork, dinfo);
+  x.launches = pht::tl_launches - l0;
   cudaMemcpyAsync(info, dinfo, sizeof(int) * (size_t)count, cudaMemcpyDeviceToHost, x.stream);
   const int rc = finish(x);
   cudaFree(buf);

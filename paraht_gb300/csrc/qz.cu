@@ -1,4 +1,5 @@
-// qz.cu -- the batched eigenvalue kernel around the QZ core in qz.cuh: one warp per pencil.
+// qz.cu -- the batched eigenvalue kernel around the QZ core in qz.cuh: a small pencil per warp, a
+// large pencil per CTA.
 #include <cuda_runtime.h>
 
 #include "launch_count.h"
@@ -6,46 +7,53 @@
 
 namespace pht {
 
-constexpr int kQzWarps = 4;  // pencils per block: one warp on each of an SM's four schedulers
-
-__global__ void __launch_bounds__(32 * kQzWarps) k_qz_eigs(const QzPencil* __restrict__ P, int count,
-                                                         QzC* __restrict__ work, int* __restrict__ info) {
-  const int w = blockIdx.x * kQzWarps + (int)(threadIdx.x >> 5);
-  if (w >= count) return;  // the whole warp leaves together
-  const int lane = threadIdx.x & 31;
-  const QzPencil p = P[w];
+__device__ void qz_pencil(const QzPencil& p, QzC* work, int* info, int idx, QzLanes L) {
   const int n = p.n;
   QzC* H = work + p.off;
   QzC* T = H + (size_t)n * n;
   QzC* alpha = T + (size_t)n * n;
   QzC* beta = alpha + n;
   // complex copies, zero below the Hessenberg / triangular structure
-  for (long long e = lane; e < (long long)n * n; e += 32) {
+  for (long long e = L.lane; e < (long long)n * n; e += L.n) {
     const int j = (int)(e / n), i = (int)(e % n);
     H[e] = qz_c(i <= j + 1 ? p.H[(size_t)j * p.ldh + i] : 0.0);
     T[e] = qz_c(i <= j ? p.T[(size_t)j * p.ldt + i] : 0.0);
   }
-  __syncwarp();
-  const int rc = qz_eigs(n, H, T, n, alpha, beta, QzLanes{lane, 32});
-  __syncwarp();
+  qz_sync(L);
+  const int rc = qz_eigs(n, H, T, n, alpha, beta, L);
+  qz_sync(L);
   if (rc == 0) {
     // beta real and nonnegative: (alpha, beta) <- (alpha conj(beta) / |beta|, |beta|)
-    for (int j = lane; j < n; j += 32) {
+    for (int j = L.lane; j < n; j += L.n) {
       const QzC b = beta[j];
       const double m = qz_abs(b);
-      const QzC a = (1.0 / m) * (alpha[j] * qz_conj(b));
+      const QzC a = alpha[j] * ((1.0 / m) * qz_conj(b));  // the unit phase first: no overflow
       p.alphar[j] = a.re;
       p.alphai[j] = a.im;
       p.beta[j] = m;
     }
   }
-  if (lane == 0) info[w] = rc;
+  if (L.lane == 0) info[idx] = rc;
 }
 
-void launch_qz_eigs(cudaStream_t s, const QzPencil* P, int count, QzC* work, int* info) {
-  if (count <= 0) return;
+__global__ void __launch_bounds__(kQzThreads, kQzMinBlocks) k_qz_eigs(const QzPencil* __restrict__ P,
+                                                        const QzBlock* __restrict__ blocks, QzC* __restrict__ work,
+                                                        int* __restrict__ info) {
+  const QzBlock b = blocks[blockIdx.x];
+  if (b.whole) {  // every thread of the CTA: the branch is uniform over the block
+    qz_pencil(P[b.pencil[0]], work, info, b.pencil[0], QzLanes{(int)threadIdx.x, kQzThreads});
+    return;
+  }
+  const int w = (int)(threadIdx.x >> 5);
+  const int idx = b.pencil[w];
+  if (idx < 0) return;  // the whole warp leaves together; warps of this kind never sync the CTA
+  qz_pencil(P[idx], work, info, idx, QzLanes{(int)(threadIdx.x & 31), 32});
+}
+
+void launch_qz_eigs(cudaStream_t s, const QzPencil* P, const QzBlock* blocks, int nblocks, QzC* work, int* info) {
+  if (nblocks <= 0) return;
   count_launch();
-  k_qz_eigs<<<(count + kQzWarps - 1) / kQzWarps, 32 * kQzWarps, 0, s>>>(P, count, work, info);
+  k_qz_eigs<<<nblocks, kQzThreads, 0, s>>>(P, blocks, work, info);
 }
 
 }  // namespace pht

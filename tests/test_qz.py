@@ -91,6 +91,24 @@ def test_hgeqz_complex_pairs_repeated_and_singular():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("sh,st", [(1e160, 1e160), (1e-160, 1e-160), (1e-300, 1e-300), (1e150, 1e-100),
+                                   (1.0, 1e-200)])
+def test_hgeqz_scaled_pencils(sh, st):
+    """Pencils scaled toward the overflow and underflow thresholds (H by sh, T by st): the core
+    scales both by powers of two first, so the eigenvalues (those of the unscaled pencil times
+    sh / st) keep full accuracy.  Compared after dividing by the largest modulus."""
+    import paraht_gb300 as ph
+
+    H, T = _pencil(60, 77)
+    alpha, beta, info = ph.hgeqz_eigs(H * sh, T * st)
+    assert info == 0
+    ref = sla.eigvals(H * sh, T * st)
+    m = np.max(np.abs(ref))
+    assert np.isfinite(m) and m > 0.0
+    assert eig_mismatch((alpha / beta) / m, ref / m) <= TOL
+
+
+@pytest.mark.gpu
 def test_hgeqz_of_the_reduction_matches_dggev_of_the_pencil():
     """The eigenvalues of the library's reduced pencil against DGGEV of the original pencil (both
     precision paths), the whole pipeline reduction -> QZ on the GPU."""
@@ -109,13 +127,14 @@ def test_hgeqz_of_the_reduction_matches_dggev_of_the_pencil():
 
 @pytest.mark.gpu
 def test_hgeqz_batched_device_entry_matches_host_entry():
-    """A batch of 40 pencils of mixed sizes through the device entry (one warp per pencil) gives
-    bitwise the host entry's results, pencil by pencil, and DGGEV's eigenvalues."""
+    """A batch of 40 pencils of mixed sizes through the device entry (a warp per pencil below
+    n = 128, a CTA per pencil from there) gives bitwise the host entry's results, pencil by pencil,
+    and DGGEV's eigenvalues."""
     torch = pytest.importorskip("torch")
     import paraht_gb300 as ph
 
     rng = np.random.default_rng(3)
-    ns = [int(v) for v in rng.integers(1, 120, 40)]
+    ns = [int(v) for v in rng.integers(1, 300, 40)]
     pens = [_pencil(n, 1000 + i) for i, n in enumerate(ns)]
     ctx = ph.Context()
     try:
