@@ -66,3 +66,12 @@ def test_eig_mismatch_greedy_matching():
     assert bench.eig_mismatch([0.5], [0.6]) == pytest.approx(0.1)           # absolute below |lambda| = 1
     assert bench.eig_mismatch([1.0, np.inf], [1.0, 2.0]) == float("inf")    # an infinite one unmatched
     assert bench.eig_mismatch([1.0], [1.0, 2.0]) == float("inf")
+
+
+def test_reference_arm_qz_line():
+    """--workload qz1216: DHGEQZ on every host core over the whole batch of 1216 pencils."""
+    d = _run("--workload", "qz1216", "--impl", "reference", "--steps", "1", "--warmup", "0")
+    assert d["impl"] == "reference" and d["unit"] == "pencils/s" and d["higher_is_better"] is True
+    cb = d["cpu_baseline"]
+    assert d["value"] > 0 and cb["value"] == d["value"] and cb["cores"] == (os.cpu_count() or 1)
+    assert 0 < cb["one_core"] <= d["value"] * 1.5
