@@ -958,7 +958,7 @@ def run_qz(args, rank: int, world: int, local: int):
     n3 = statistics.mean(float(n) ** 3 for n in sizes)
     metric = "QZ eigenvalues: pencils/s, 1216 Hessenberg-triangular pencils n~U{32..256}"
     workload = (f"{count} random Hessenberg-triangular pencils, n ~U{{{lo}..{hi}}} (seeded), eigenvalues only, "
-                "one paraht_hgeqz_eigs_d call (complex single-shift QZ, a warp per pencil below n=128, a 2-warp CTA from there)")
+                "one paraht_hgeqz_eigs_d call (real double-shift QZ, a warp per pencil below n=128, a 2-warp CTA from there)")
 
     def cpu_rate(nsample):
         """DHGEQZ on all host cores over the whole batch, and on one core over its first nsample
@@ -1063,7 +1063,7 @@ def run_qz(args, rank: int, world: int, local: int):
             "e2e": {"value": e2e_v, "unit": "pencils/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
             "roofline": {"bound": "fp64", "achieved": None, "peak": None, "unit": None, "frac": None,
-                         "traffic": None, "kernel": "k_qz_eigs: a warp or a 2-warp CTA per pencil; complex rotations "
+                         "traffic": None, "kernel": "k_qz_eigs: a warp or a 2-warp CTA per pencil; 3 x 3 reflectors "
                                                       "bound by the FP64 issue rate (one warp instruction per "
                                                       "scheduler every ~64 cycles); flops not counted"},
             "check": check, "cpu_baseline": cpu, "clocks": sampler.summary(),

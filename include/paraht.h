@@ -212,16 +212,17 @@ int paraht_gghd3(char compq, char compz, int n, int ilo, int ihi, double* A, int
  * reference, whose driver stops at the reduced pencil, src/profilereduction.f90:156).
  * For i < count: H[i] (n[i] x n[i], leading dimension ldh[i]) upper Hessenberg and T[i] (ldt[i])
  * upper triangular, read only (entries below the structure are ignored).  Eigenvalue j of pencil
- * i is (alphar[i][j] + i alphai[i][j]) / beta[i][j] with beta >= 0, in the order of the Schur
- * form's diagonal.  Complex single-shift QZ (Moler-Stewart, Wilkinson shifts), one warp per
- * pencil: the eigenvalues of a real pencil come out with rounding-level imaginary parts where
- * DHGEQZ returns exact zeros and exact conjugate pairs.  info[i] (host array): 0; 1 when a
- * diagonal entry of T is at most eps ||T||_F (an infinite or nearly infinite eigenvalue: not
- * supported, that pencil's outputs are not written); 2 when 30 n[i] sweeps did not converge.
- * _d: host arrays of device pointers, run on the context's stream and synchronised; the plain
- * form takes host arrays on this thread's default context.  Status: 0; -2 count < 0, -3 an
- * n < 0 (or null n), -4 .. -10 a null pointer among H, ldh, T, ldt, alphar, alphai, beta (ldh,
- * ldt: or below max(1, n)), -11 null info; else a PARAHT_ERR_ code (both forms). ---- */
+ * i is (alphar[i][j] + i alphai[i][j]) / beta[i][j] with beta >= 0, in the order the iteration
+ * deflates them; beta = 0 marks an infinite eigenvalue (T singular).  Real double-shift QZ
+ * (Moler-Stewart, as DHGEQZ), a warp per pencil below n = 128 and a 2-warp CTA from there: real
+ * eigenvalues have alphai exactly 0, complex ones come as adjacent exact conjugate pairs
+ * (positive imaginary part first).  A diagonal entry of T at most eps ||T||_F counts as zero.
+ * info[i] (host array): 0, or 2 when 30 n[i] sweeps did not converge (that pencil's outputs are
+ * then incomplete).  _d: host arrays of device pointers, run on the context's stream and
+ * synchronised; the plain form takes host arrays on this thread's default context.  Status: 0;
+ * -2 count < 0, -3 an n < 0 (or null n), -4 .. -10 a null pointer among H, ldh, T, ldt, alphar,
+ * alphai, beta (ldh, ldt: or below max(1, n)), -11 null info; else a PARAHT_ERR_ code (both
+ * forms). ---- */
 int paraht_hgeqz_eigs_d(paraht_ctx ctx, int count, const int* n, const double* const* H, const int* ldh,
                         const double* const* T, const int* ldt, double* const* alphar, double* const* alphai,
                         double* const* beta, int* info);

@@ -123,13 +123,13 @@ def gghd3(compq, compz, ilo, ihi, A, B, Q, Z, r=16, p=4, nq=16, flags=0):
 
 
 def hgeqz_eigs(H, T):
-    """Generalized eigenvalues of Hessenberg-triangular pencils by the QZ iteration on the GPU
-    (LAPACK DHGEQZ with JOB='E'; paraht_hgeqz_eigs), the step after the reduction.  H, T: one
-    pair of float64 arrays (H upper Hessenberg, T upper triangular; entries below ignored) or two
-    lists of them, reduced together.  Returns (alpha, beta, info) for one pair, else a list of
-    them: alpha complex, beta real >= 0, eigenvalue alpha / beta; info 1 (T has a negligible
-    diagonal entry: infinite eigenvalues are not supported) or 2 (no convergence) leave alpha and
-    beta None."""
+    """Generalized eigenvalues of Hessenberg-triangular pencils by the real double-shift QZ
+    iteration on the GPU (LAPACK DHGEQZ with JOB='E'; paraht_hgeqz_eigs), the step after the
+    reduction.  H, T: one pair of float64 arrays (H upper Hessenberg, T upper triangular; entries
+    below ignored) or two lists of them, reduced together.  Returns (alpha, beta, info) for one
+    pair, else a list of them: alpha complex (real eigenvalues with zero imaginary part, complex
+    ones as adjacent conjugate pairs), beta real >= 0, eigenvalue alpha / beta (infinite where
+    beta = 0); info 2 (no convergence) leaves alpha and beta None."""
     single = not isinstance(H, (list, tuple))
     Hs = [np.asfortranarray(h, dtype=np.float64) for h in ([H] if single else H)]
     Ts = [np.asfortranarray(t, dtype=np.float64) for t in ([T] if single else T)]
@@ -225,7 +225,7 @@ class Context:
 
     def hgeqz_eigs_d(self, ns, Hs, ldhs, Ts, ldts, alphars, alphais, betas):
         """QZ eigenvalues of Hessenberg-triangular pencils in device memory (paraht_hgeqz_eigs_d);
-        returns the per-pencil info list (0, 1 unsupported, 2 no convergence)."""
+        returns the per-pencil info list (0, or 2 for no convergence)."""
         cnt = len(ns)
         IA, PA = C.c_int * cnt, C.c_void_p * cnt
         info = IA()

@@ -17,7 +17,7 @@
 #include "paraht_impl.h"
 #include "paraht_internal.cuh"
 #include "s2_common.cuh"
-#include "qz.cuh"
+#include "qz_real.cuh"
 #include "split_apply.cuh"
 
 namespace pht {
@@ -1031,7 +1031,7 @@ extern "C" int paraht_hgeqz_eigs_d(paraht_ctx c, int count, const int* n, const 
   auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
   const size_t tab_b = up(sizeof(pht::QzPencil) * (size_t)count), info_b = up(sizeof(int) * (size_t)count);
   const size_t blk_b = up(sizeof(pht::QzBlock) * blocks.size());
-  const size_t bytes = tab_b + info_b + blk_b + (size_t)work * sizeof(pht::QzC);
+  const size_t bytes = tab_b + info_b + blk_b + (size_t)work * sizeof(double);
   Ctx& x = c->c;
   int prev = 0;
   cudaGetDevice(&prev);
@@ -1045,7 +1045,7 @@ extern "C" int paraht_hgeqz_eigs_d(paraht_ctx c, int count, const int* n, const 
   auto* dtab = reinterpret_cast<pht::QzPencil*>(buf);
   auto* dinfo = reinterpret_cast<int*>(buf + tab_b);
   auto* dblk = reinterpret_cast<pht::QzBlock*>(buf + tab_b + info_b);
-  auto* dwork = reinterpret_cast<pht::QzC*>(buf + tab_b + info_b + blk_b);
+  auto* dwork = reinterpret_cast<double*>(buf + tab_b + info_b + blk_b);
   cudaMemcpyAsync(dtab, tab.data(), sizeof(pht::QzPencil) * (size_t)count, cudaMemcpyHostToDevice, x.stream);
   cudaMemcpyAsync(dblk, blocks.data(), sizeof(pht::QzBlock) * blocks.size(), cudaMemcpyHostToDevice, x.stream);
   const long long l0 = pht::tl_launches;

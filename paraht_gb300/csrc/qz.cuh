@@ -332,8 +332,9 @@ __host__ __device__ inline int qz_eigs(int n, QzC* H, QzC* T, int ld, QzC* alpha
 
 namespace pht {
 
-// One pencil of a batched eigenvalue call: real H, T (device, column-major), the outputs, and the
-// offset of its complex scratch (H, T, alpha, beta: qz_work_elems(n) entries) in the call's buffer.
+// One pencil of a batched eigenvalue call (the kernel in qz.cu runs the real double-shift core of
+// qz_real.cuh on it): real H, T (device, column-major), the outputs, and the offset of its scratch
+// (copies of H and T: qz_work_elems(n) doubles) in the call's buffer.
 struct QzPencil {
   const double* H;
   const double* T;
@@ -343,12 +344,12 @@ struct QzPencil {
   long long off;
   int n, ldh, ldt, pad;
 };
-inline long long qz_work_elems(int n) { return 2ll * n * n + 2ll * n; }
+inline long long qz_work_elems(int n) { return 2ll * n * n; }
 // A CTA of kQzThreads threads runs either one pencil of n >= kQzWholeMin on both its warps (the
 // row and column passes on two of the SM's schedulers) or two smaller pencils, one per warp;
 // kQzMinBlocks CTAs fit on an SM (at most 168 registers a thread).  pencil[w] < 0: no pencil for
-// warp w.  Measured on GB300 against four-warp CTAs and one warp per pencil: 967, 797 and 893
-// pencils/s on 1216 pencils n ~ U{32..256}.
+// warp w.  Measured on GB300 with the complex single-shift core against four-warp CTAs and one
+// warp per pencil: 967, 797 and 893 pencils/s on 1216 pencils n ~ U{32..256}.
 constexpr int kQzThreads = 64;
 constexpr int kQzMinBlocks = 6;
 constexpr int kQzWholeMin = 128;
@@ -358,6 +359,6 @@ struct QzBlock {
 };
 static_assert(kQzThreads % 32 == 0 && kQzThreads / 32 <= 4, "a CTA holds at most four warps' pencils");
 // One CTA per block entry on stream s; info[i] receives qz_eigs's status for pencil i.
-void launch_qz_eigs(cudaStream_t s, const QzPencil* P, const QzBlock* blocks, int nblocks, QzC* work, int* info);
+void launch_qz_eigs(cudaStream_t s, const QzPencil* P, const QzBlock* blocks, int nblocks, double* work, int* info);
 
 }  // namespace pht
