@@ -1059,13 +1059,13 @@ def run_qz(args, rank: int, world: int, local: int):
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c128", "data": "synthetic",
             "config": {"workload": workload, "pencils": count, "n_lo": lo, "n_hi": hi,
-                       "l2": "working set about 1 GB of complex copies, above L2"},
+                       "l2": "working set about 0.5 GB of copies, above L2"},
             "e2e": {"value": e2e_v, "unit": "pencils/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
             "roofline": {"bound": "fp64", "achieved": None, "peak": None, "unit": None, "frac": None,
-                         "traffic": None, "kernel": "k_qz_eigs: a warp or a 2-warp CTA per pencil; 3 x 3 reflectors "
-                                                      "bound by the FP64 issue rate (one warp instruction per "
-                                                      "scheduler every ~64 cycles); flops not counted"},
+                         "traffic": None, "kernel": "k_qz_eigs: a warp or a 2-warp CTA per pencil; each pencil a serial "
+                                                      "chain of dependent 3 x 3 reflectors, bound by its latency "
+                                                      "and the FP64 issue rate; flops not counted"},
             "check": check, "cpu_baseline": cpu, "clocks": sampler.summary(),
         }), flush=True)
     if dist_on:
