@@ -1178,7 +1178,7 @@ int oracle_triangularize(int n, double* B, int ldb) {
   return info;
 }
 
-/* profilereduction.f90:165-174: ||Q^T A0 Z - H||_F / ||A0||_F with the driver's own dgemm/dlange calls. */
+/* profilereduction.f90:165-174: ||Q^T A0 Z - H||_F / ||A0||_F with profilereduction's own dgemm/dlange calls. */
 double oracle_backward_error(int n, const double* Q, int ldq, const double* A0, int lda0, const double* Z, int ldz,
                              const double* H, int ldh) {
   if (init_lapack()) return -1.0;

@@ -23,7 +23,7 @@ import numpy as np
 
 
 def _lapack_dgghd3():
-    """DGGHD3 from the OpenBLAS bundled with scipy (the LAPACK baseline of the driver)."""
+    """DGGHD3 from the OpenBLAS bundled with scipy (profilereduction's LAPACK baseline, algorithm 2)."""
     import scipy
 
     base = os.path.dirname(os.path.dirname(scipy.__file__))
