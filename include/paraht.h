@@ -212,8 +212,9 @@ int paraht_gghd3(char compq, char compz, int n, int ilo, int ihi, double* A, int
  * reference, whose driver stops at the reduced pencil, src/profilereduction.f90:156).
  * For i < count: H[i] (n[i] x n[i], leading dimension ldh[i]) upper Hessenberg and T[i] (ldt[i])
  * upper triangular, read only (entries below the structure are ignored).  Eigenvalue j of pencil
- * i is (alphar[i][j] + i alphai[i][j]) / beta[i][j] with beta >= 0, in the order the iteration
- * deflates them; beta = 0 marks an infinite eigenvalue (T singular).  Real double-shift QZ
+ * i is (alphar[i][j] + i alphai[i][j]) / beta[i][j] with beta >= 0, at its position j on the
+ * diagonal of the final quasi-triangular pencil (as DHGEQZ orders them); beta = 0 marks an
+ * infinite eigenvalue (T singular).  Real double-shift QZ
  * (Moler-Stewart, as DHGEQZ), a warp per pencil below n = 128 and a 2-warp CTA from there: real
  * eigenvalues have alphai exactly 0, complex ones come as adjacent exact conjugate pairs
  * (positive imaginary part first).  A diagonal entry of T at most eps ||T||_F counts as zero.
