@@ -5,7 +5,8 @@
 ! `rht2ht_givens` with exactly the argument lists of the reference (src/ab2rht.f90:8-13,
 ! src/rht2ht.f90:1346-1351, src/rht2ht.f90:696-700), so a
 ! caller such as src/profilereduction.f90 only needs to be recompiled against this file and
-! linked with -lparaht.  Arrays stay on the host; each call copies them to the GPU, reduces and
+! linked with -lparaht.  Module `paraht_qz` adds `hgeqz_eigs`, the eigenvalues of the reduced
+! pencil (no counterpart in the reference).  Arrays stay on the host; each call copies them to the GPU, reduces and
 ! copies them back.  An optional trailing INFO argument returns the library status (0 = ok,
 ! -i = i-th argument invalid, <= -1000 = PARAHT_ERR_*); without it a failure is reported on
 ! standard error (the reference itself performs no error reporting).
@@ -15,7 +16,7 @@
 !   gfortran ... your_program.f90 paraht_gb300.o -L<dir of libparaht.so> -lparaht -Wl,-rpath,<dir>
 
 module paraht_c
-   use iso_c_binding, only: c_int, c_double, c_char
+   use iso_c_binding, only: c_int, c_double, c_char, c_ptr
    implicit none
    interface
       integer(c_int) function paraht_ab2rht(n, A, lda, B, ldb, Q, ldq, Z, ldz, nb, p, time_components) &
@@ -54,6 +55,15 @@ module paraht_c
          integer(c_int), value :: n, ilo, ihi, lda, ldb, ldq, ldz, r, p, nq, flags
          real(c_double) :: A(*), B(*), Q(*), Z(*)
       end function paraht_gghd3
+
+      ! QZ eigenvalues of count Hessenberg-triangular pencils (arrays of per-pencil pointers)
+      integer(c_int) function paraht_hgeqz_eigs(count, n, H, ldh, T, ldt, alphar, alphai, beta, info) &
+         bind(C, name="paraht_hgeqz_eigs")
+         import :: c_int, c_ptr
+         integer(c_int), value :: count
+         integer(c_int) :: n(*), ldh(*), ldt(*), info(*)
+         type(c_ptr) :: H(*), T(*), alphar(*), alphai(*), beta(*)
+      end function paraht_hgeqz_eigs
    end interface
 
 contains
@@ -119,3 +129,39 @@ contains
       call paraht_report('rht2ht_givens', status, info)
    end subroutine rht2ht_givens
 end module rht2ht
+
+module paraht_qz
+   use paraht_c
+   use iso_c_binding, only: c_int, c_ptr, c_loc
+   implicit none
+contains
+   ! Eigenvalues of one Hessenberg-triangular pencil (H, T) on the GPU, the step after the
+   ! reduction (LAPACK DHGEQZ with JOB='E', COMPQ=COMPZ='N'; no counterpart in the reference):
+   ! eigenvalue j is (alphar(j) + i alphai(j)) / beta(j), beta(j) >= 0, beta(j) = 0 for an
+   ! infinite one.  H and T are not modified.  info: 0, 2 (no convergence), else a library status.
+   subroutine hgeqz_eigs(n, H, ldh, T, ldt, alphar, alphai, beta, info)
+      integer, intent(in) :: n, ldh, ldt
+      double precision, intent(in), target :: H(ldh,*), T(ldt,*)
+      double precision, intent(out), target :: alphar(*), alphai(*), beta(*)
+      integer, intent(out), optional :: info
+      integer(c_int) :: status, cn(1), cldh(1), cldt(1), cinfo(1)
+      type(c_ptr) :: pH(1), pT(1), pr(1), pi(1), pb(1)
+      if (n < 0) then
+         status = -3
+      else if (n == 0) then
+         status = 0
+      else
+         cn(1) = int(n, c_int)
+         cldh(1) = int(ldh, c_int)
+         cldt(1) = int(ldt, c_int)
+         pH(1) = c_loc(H(1,1))
+         pT(1) = c_loc(T(1,1))
+         pr(1) = c_loc(alphar(1))
+         pi(1) = c_loc(alphai(1))
+         pb(1) = c_loc(beta(1))
+         status = paraht_hgeqz_eigs(1_c_int, cn, pH, cldh, pT, cldt, pr, pi, pb, cinfo)
+         if (status == 0) status = cinfo(1)
+      end if
+      call paraht_report('hgeqz_eigs', status, info)
+   end subroutine hgeqz_eigs
+end module paraht_qz
