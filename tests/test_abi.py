@@ -133,3 +133,33 @@ def test_gghd3_leading_dimension_and_parameter_errors():
     assert L.paraht_gghd3(b"V", b"I", 10, 1, 10, p, 10, p, 10, p, 5, p, 10, 4, 2, 2, 0) == -11
     assert L.paraht_gghd3(b"I", b"I", 10, 1, 10, p, 10, p, 10, p, 10, p, 10, 4, 1, 2, 0) == -15
     assert L.paraht_gghd3(b"I", b"I", 10, 1, 10, p, 10, p, 10, p, 10, p, 10, 4, 2, 5, 0) == -16
+
+
+def _header_arg_counts():
+    """Number of parameters of every function the header declares."""
+    with open(os.path.join(os.path.dirname(__file__), "..", "include", "paraht.h")) as f:
+        src = re.sub(r"/\*.*?\*/", "", f.read(), flags=re.S)
+    out = {}
+    for name, params in re.findall(r"\b(paraht_\w+)\s*\(([^;{]*?)\)\s*;", src, flags=re.S):
+        params = params.strip()
+        out[name] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
+def test_fortran_interfaces_match_the_header():
+    """The Fortran module (paraht_gb300/fortran/paraht_gb300.f90, not compiled here: no Fortran
+    compiler in the image) binds each C entry by name with as many dummy arguments as the header's
+    prototype has parameters, and only entries the library exports."""
+    path = os.path.join(os.path.dirname(__file__), "..", "paraht_gb300", "fortran", "paraht_gb300.f90")
+    with open(path) as f:
+        src = re.sub(r"!.*", "", f.read())
+    src = src.replace("&\n", " ")
+    binds = re.findall(r"function\s+(\w+)\s*\(([^)]*)\)\s*bind\(\s*C\s*,\s*name\s*=\s*\"(\w+)\"\s*\)", src, flags=re.I)
+    assert len(binds) >= 6
+    counts = _header_arg_counts()
+    L = _lib.lib()
+    for fname, args, cname in binds:
+        assert fname.lower() == cname.lower()
+        assert cname in counts, cname
+        assert len([a for a in args.split(",") if a.strip()]) == counts[cname], cname
+        assert hasattr(L, cname), cname
