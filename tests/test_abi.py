@@ -163,3 +163,33 @@ def test_fortran_interfaces_match_the_header():
         assert cname in counts, cname
         assert len([a for a in args.split(",") if a.strip()]) == counts[cname], cname
         assert hasattr(L, cname), cname
+
+
+def test_header_is_plain_c_and_links(tmp_path):
+    """include/paraht.h is valid C99 on its own, and a C program built against it links with
+    libparaht.so and calls it (no GPU needed for the calls made: version, strerror, argument
+    rejection)."""
+    import shutil
+    import subprocess
+
+    gcc = shutil.which("gcc")
+    if not gcc:
+        pytest.skip("gcc missing")
+    _lib.lib()  # the library is built and current
+    src = tmp_path / "caller.c"
+    src.write_text(
+        '#include "paraht.h"\n#include <stdio.h>\n'
+        "int main(void) {\n"
+        "  int n = 4, ld = 4, info = 0;\n"
+        "  if (paraht_version() != 100) return 1;\n"
+        "  if (paraht_hgeqz_eigs(-1, &n, 0, &ld, 0, &ld, 0, 0, 0, &info) != -2) return 2;\n"
+        "  if (paraht_reduce_d(0, 4, 0, 4, 0, 4, 0, 4, 0, 4, 2, 2, 2, 0) != PARAHT_ERR_BAD_CTX) return 3;\n"
+        '  printf("%s\\n", paraht_strerror(PARAHT_ERR_ALLOC));\n'
+        "  return 0;\n}\n")
+    exe = tmp_path / "caller"
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    r = subprocess.run([gcc, "-std=c99", "-Wall", "-Werror", "-pedantic", "-I", os.path.join(ROOT, "include"), str(src),
+                        "-o", str(exe), "-L", libdir, "-lparaht", "-Wl,-rpath," + libdir], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and r.stdout.strip() == "allocation failed", (r.returncode, r.stdout, r.stderr)
