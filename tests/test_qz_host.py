@@ -145,3 +145,37 @@ def test_real_qz_graded_reduced_pencil_backward_stable(qzlib, oracle):
     worst = max(np.linalg.svd(b * H - a * T, compute_uv=False)[-1] / (abs(b) * nh + abs(a) * nt)
                 for a, b in zip(ar + 1j * ai, be))
     assert worst <= 1e-14
+
+
+@pytest.mark.timeout(600)
+def test_real_qz_randomized_backward_stability(qzlib):
+    """Seeded random pencils of mixed structure (sizes 1-60; zero diagonal entries of T at random
+    places; exact zeros on H's subdiagonal; H and T scaled by powers of ten between 1e-100 and
+    1e100; 1 or 4 lanes): every eigenvalue's backward error
+    sigma_min(beta H - alpha T) / (|beta| ||H|| + |alpha| ||T||) within a few eps, and beta >= 0,
+    real eigenvalues or exact conjugate pairs."""
+    rng = np.random.default_rng(2024)
+    worst, where = 0.0, None
+    for case in range(100):
+        n = int(rng.integers(1, 61))
+        H, T = _pencil(n, 5000 + case)
+        if n > 1 and case % 3 == 0:
+            z = rng.integers(0, n, int(rng.integers(1, 4)))
+            T[z, z] = 0.0
+        if n > 2 and case % 4 == 1:
+            k = int(rng.integers(1, n))
+            H[k, k - 1] = 0.0
+        H, T = H * 10.0 ** rng.integers(-100, 101), T * 10.0 ** rng.integers(-100, 101)
+        rc, ar, ai, be = _eigs(qzlib, (1, 4)[case % 2], H, T)
+        assert rc == 0, case
+        assert np.all(be >= 0.0) and _pairs_exact(ar, ai), case
+        nh, nt = np.linalg.norm(H, 2), np.linalg.norm(T, 2)
+        for a, b in zip(ar + 1j * ai, be):
+            bb, aa = b * nh, a * nt  # the pair for the normalised pencil (H / nh, T / nt)
+            sc = max(abs(bb), abs(aa))
+            sv = np.linalg.svd((bb / sc) * (H / nh) - (aa / sc) * (T / nt), compute_uv=False)[-1]
+            err = sv * sc / (abs(bb) + abs(aa))
+            if err > worst:
+                worst, where = err, case
+    assert worst <= 1e-14, (worst, where)
+    print("worst backward error %.2e (case %s)" % (worst, where))
